@@ -1,0 +1,118 @@
+"""ctypes loader for libexoblas_gb300.so and the table of its C signatures.
+
+The library is built in-tree by exoblas_gb300.build (or __graft_entry__.build)
+and loaded from this package directory.  There is no CPU fallback: importing
+a function whose library is missing raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libexoblas_gb300.so"
+
+# C type codes used in the signature table
+_T = {
+    "i": C.c_int,
+    "f": C.c_float,
+    "d": C.c_double,
+    "p": C.c_void_p,
+    "v": None,
+    "s": C.c_char_p,
+    "u": C.c_ulonglong,
+}
+
+L1 = {
+    # name: (restype, argtypes)  -- pointers are 'p'
+    "exo_sasum": ("f", "ipi"),
+    "exo_dasum": ("d", "ipi"),
+    "exo_saxpy": ("v", "ifpipi"),
+    "exo_daxpy": ("v", "idpipi"),
+    "exo_sdot": ("f", "ipipi"),
+    "exo_ddot": ("d", "ipipi"),
+    "exo_dsdot": ("d", "ipipi"),
+    "exo_sdsdot": ("f", "ifpipi"),
+    "exo_scopy": ("v", "ipipi"),
+    "exo_dcopy": ("v", "ipipi"),
+    "exo_sswap": ("v", "ipipi"),
+    "exo_dswap": ("v", "ipipi"),
+    "exo_sscal": ("v", "ifpi"),
+    "exo_dscal": ("v", "idpi"),
+    "exo_srot": ("v", "ipipiff"),
+    "exo_drot": ("v", "ipipidd"),
+    "exo_srotm": ("v", "ipipip"),
+    "exo_drotm": ("v", "ipipip"),
+}
+L2 = {
+    "exo_sgemv": ("v", "iiiifpipifpi"),
+    "exo_dgemv": ("v", "iiiidpipidpi"),
+    "exo_sger": ("v", "iiifpipipi"),
+    "exo_dger": ("v", "iiidpipipi"),
+    "exo_ssymv": ("v", "iiifpipifpi"),
+    "exo_dsymv": ("v", "iiidpipidpi"),
+    "exo_ssyr": ("v", "iiifpipi"),
+    "exo_dsyr": ("v", "iiidpipi"),
+    "exo_ssyr2": ("v", "iiifpipipi"),
+    "exo_dsyr2": ("v", "iiidpipipi"),
+    "exo_strmv": ("v", "iiiiipipi"),
+    "exo_dtrmv": ("v", "iiiiipipi"),
+    "exo_strsv": ("v", "iiiiipipi"),
+    "exo_dtrsv": ("v", "iiiiipipi"),
+}
+L3 = {
+    "exo_sgemm": ("v", "iiiiiifpipifpi"),
+    "exo_dgemm": ("v", "iiiiiidpipidpi"),
+    "exo_ssymm": ("v", "iiiiifpipifpi"),
+    "exo_dsymm": ("v", "iiiiidpipidpi"),
+    "exo_ssyrk": ("v", "iiiiifpifpi"),
+    "exo_dsyrk": ("v", "iiiiidpidpi"),
+}
+EXTRA = {
+    "exoblas_get_status": ("i", ""),
+    "exoblas_status_string": ("s", "i"),
+    "exoblas_set_error_handler": ("v", "p"),
+    "exoblas_set_stream": ("i", "p"),
+    "exoblas_get_stream": ("p", ""),
+    "exoblas_set_blocking": ("i", "i"),
+    "exoblas_synchronize": ("i", ""),
+    "exoblas_set_precision": ("i", "i"),
+    "exoblas_get_precision": ("i", ""),
+    "exoblas_kernel_launches": ("u", ""),
+    "exoblas_sasum_device": ("i", "ipip"),
+    "exoblas_dasum_device": ("i", "ipip"),
+    "exoblas_sdot_device": ("i", "ipipip"),
+    "exoblas_ddot_device": ("i", "ipipip"),
+    "exoblas_dsdot_device": ("i", "ipipip"),
+}
+
+SIGNATURES = {**L1, **L2, **L3, **EXTRA}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+                "(there is no CPU fallback)"
+            )
+        mode = getattr(os, "RTLD_GLOBAL", 0)
+        lib_ = C.CDLL(str(LIB_PATH), mode=mode)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib_, name, None)
+            if fn is None:
+                continue
+            fn.restype = _T[res]
+            fn.argtypes = [_T[a] for a in args]
+        _lib = lib_
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    """Names from the signature table that the loaded library exports."""
+    L = lib()
+    return [n for n in SIGNATURES if hasattr(L, n)]

@@ -1,0 +1,353 @@
+// exo_<p><op> level-2 and level-3 entry points (C ABI).  Flag handling is
+// the reference's: each proc tests one flag value and takes the other branch
+// for anything else (e.g. gemv.py:15 tests TransA == NoTrans, trmv.py:23
+// tests Diag == Unit, trsv.py:29 tests Diag == NonUnit), so the same
+// permissive mapping is used here.  Arguments the reference never checks
+// but that would make a GPU kernel read or write out of bounds (negative
+// sizes, a leading dimension smaller than the row length, a zero output
+// stride) are rejected with EXOBLAS_INVALID_VALUE and leave outputs untouched.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace exb {
+
+template <typename T>
+static inline T *rebase(T *p, long n, long inc) {
+  return inc < 0 ? p + (1 - n) * inc : p;
+}
+
+static void row_major(int order) {
+  if (order != kRowMajor) fail(EXOBLAS_UNSUPPORTED_ORDER, "Order must be CblasRowMajor");
+}
+static void nonneg(long v, const char *what) {
+  if (v < 0) fail(EXOBLAS_INVALID_VALUE, what);
+}
+static void ld_ok(long ld, long cols, const char *what) {
+  if (ld < (cols > 1 ? cols : 1)) fail(EXOBLAS_INVALID_VALUE, what);
+}
+static void inc_ok(long inc, const char *what) {
+  if (inc == 0) fail(EXOBLAS_INVALID_VALUE, what);
+}
+
+// Level-3 dispatch on the thread's precision mode.
+template <typename T>
+static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb,
+                          T beta, T *C, long ldc) {
+  l3::gemm_simt<T>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+
+// ------------------------------------------------------------------ level 2
+
+// test/level2/gemv/exo_gemv_wrapper.h:7-39
+template <typename T>
+static void gemv_entry(const char *fn, int order, int TransA, int M, int N, T alpha, const T *A, int lda, const T *X,
+                       int incX, T beta, T *Y, int incY) {
+  guarded(fn, [&] {
+    row_major(order);
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    const bool trans = TransA != kNoTrans;
+    const long ylen = trans ? N : M, xlen = trans ? M : N;
+    if (ylen == 0) return;
+    if (M > 0 && N > 0) ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incY, "incY == 0");
+    if (xlen > 0) inc_ok(incX, "incX == 0");
+    X = rebase(X, xlen, incX);
+    Y = rebase(Y, ylen, incY);
+    Stager st;
+    const T *dA = st.mat(A, M, N, lda, false);
+    const T *dx = st.vec(X, xlen, incX, false);
+    T *dy = st.vec(Y, ylen, incY, true);
+    l2::gemv<T>(trans, M, N, alpha, dA, lda, dx, incX, beta, dy, incY);
+    st.finish();
+  });
+}
+
+// test/level2/ger/exo_ger_wrapper.h:7-34 (Order not checked)
+template <typename T>
+static void ger_entry(const char *fn, int M, int N, T alpha, const T *X, int incX, const T *Y, int incY, T *A,
+                      int lda) {
+  guarded(fn, [&] {
+    if (alpha == T(0)) return;
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    if (M == 0 || N == 0) return;
+    ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incX, "incX == 0");
+    inc_ok(incY, "incY == 0");
+    X = rebase(X, M, incX);
+    Y = rebase(Y, N, incY);
+    Stager st;
+    const T *dx = st.vec(X, M, incX, false);
+    const T *dy = st.vec(Y, N, incY, false);
+    T *dA = st.mat(A, M, N, lda, true);
+    l2::ger<T>(M, N, alpha, dx, incX, dy, incY, dA, lda);
+    st.finish();
+  });
+}
+
+// test/level2/symv/exo_symv_wrapper.h:7-34
+template <typename T>
+static void symv_entry(const char *fn, int order, int Uplo, int N, T alpha, const T *A, int lda, const T *X, int incX,
+                       T beta, T *Y, int incY) {
+  guarded(fn, [&] {
+    row_major(order);
+    nonneg(N, "N < 0");
+    if (N == 0) return;
+    ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incX, "incX == 0");
+    inc_ok(incY, "incY == 0");
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+    Stager st;
+    const T *dA = st.mat(A, N, N, lda, false);
+    const T *dx = st.vec(X, N, incX, false);
+    T *dy = st.vec(Y, N, incY, true);
+    l2::symv<T>(Uplo == kUpper, N, alpha, dA, lda, dx, incX, beta, dy, incY);
+    st.finish();
+  });
+}
+
+// test/level2/syr/exo_syr_wrapper.h:5-32
+template <typename T>
+static void syr_entry(const char *fn, int order, int Uplo, int N, T alpha, const T *X, int incX, T *A, int lda) {
+  guarded(fn, [&] {
+    row_major(order);
+    if (alpha == T(0)) return;
+    nonneg(N, "N < 0");
+    if (N == 0) return;
+    ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incX, "incX == 0");
+    X = rebase(X, N, incX);
+    Stager st;
+    const T *dx = st.vec(X, N, incX, false);
+    T *dA = st.mat(A, N, N, lda, true);
+    l2::syr<T>(Uplo == kUpper, N, alpha, dx, incX, dA, lda);
+    st.finish();
+  });
+}
+
+// test/level2/syr2/exo_syr2_wrapper.h:5-36 (Order not checked)
+template <typename T>
+static void syr2_entry(const char *fn, int Uplo, int N, T alpha, const T *X, int incX, const T *Y, int incY, T *A,
+                       int lda) {
+  guarded(fn, [&] {
+    if (alpha == T(0)) return;
+    nonneg(N, "N < 0");
+    if (N == 0) return;
+    ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incX, "incX == 0");
+    inc_ok(incY, "incY == 0");
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+    Stager st;
+    const T *dx = st.vec(X, N, incX, false);
+    const T *dy = st.vec(Y, N, incY, false);
+    T *dA = st.mat(A, N, N, lda, true);
+    l2::syr2<T>(Uplo == kUpper, N, alpha, dx, incX, dy, incY, dA, lda);
+    st.finish();
+  });
+}
+
+// test/level2/trmv/exo_trmv_wrapper.h:7-29 (unit diagonal iff Diag == Unit, trmv.py:23)
+// test/level2/trsv/exo_trsv_wrapper.h:7-29 (divides iff Diag == NonUnit, trsv.py:29)
+template <typename T, bool SOLVE>
+static void tr_entry(const char *fn, int order, int Uplo, int TransA, int Diag, int N, const T *A, int lda, T *X,
+                     int incX) {
+  guarded(fn, [&] {
+    row_major(order);
+    nonneg(N, "N < 0");
+    if (N == 0) return;
+    ld_ok(lda, N, "lda < max(1, N)");
+    inc_ok(incX, "incX == 0");
+    X = rebase(X, N, incX);
+    Stager st;
+    const T *dA = st.mat(A, N, N, lda, false);
+    T *dx = st.vec(X, N, incX, true);
+    const bool upper = Uplo == kUpper, trans = TransA != kNoTrans;
+    if (SOLVE)
+      l2::trsv<T>(upper, trans, Diag != kNonUnit, N, dA, lda, dx, incX);
+    else
+      l2::trmv<T>(upper, trans, Diag == kUnit, N, dA, lda, dx, incX);
+    st.finish();
+  });
+}
+
+// ------------------------------------------------------------------ level 3
+
+// test/level3/gemm/exo_gemm_wrapper.h:9-28
+template <typename T>
+static void gemm_entry(const char *fn, int Order, int TransA, int TransB, int M, int N, int K, T alpha, const T *A,
+                       int lda, const T *B, int ldb, T beta, T *C, int ldc) {
+  guarded(fn, [&] {
+    row_major(Order);
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    nonneg(K, "K < 0");
+    if (M == 0 || N == 0) return;
+    const bool ta = TransA != kNoTrans, tb = TransB != kNoTrans;
+    const long ar = ta ? K : M, ac = ta ? M : K, br = tb ? N : K, bc = tb ? K : N;
+    if (K > 0) {
+      ld_ok(lda, ac, "lda too small");
+      ld_ok(ldb, bc, "ldb too small");
+    }
+    ld_ok(ldc, N, "ldc < max(1, N)");
+    Stager st;
+    const T *dA = K > 0 ? st.mat(A, ar, ac, lda, false) : A;
+    const T *dB = K > 0 ? st.mat(B, br, bc, ldb, false) : B;
+    T *dC = st.mat(C, M, N, ldc, true);
+    gemm_dispatch<T>(ta, tb, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc);
+    st.finish();
+  });
+}
+
+// test/level3/symm/exo_symm_wrapper.h:9-27
+template <typename T>
+static void symm_entry(const char *fn, int Order, int Side, int Uplo, int M, int N, T alpha, const T *A, int lda,
+                       const T *B, int ldb, T beta, T *C, int ldc) {
+  guarded(fn, [&] {
+    row_major(Order);
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    if (M == 0 || N == 0) return;
+    const bool left = Side == kLeft;
+    const long ka = left ? M : N;
+    ld_ok(lda, ka, "lda too small");
+    ld_ok(ldb, N, "ldb < max(1, N)");
+    ld_ok(ldc, N, "ldc < max(1, N)");
+    Stager st;
+    const T *dA = st.mat(A, ka, ka, lda, false);
+    const T *dB = st.mat(B, M, N, ldb, false);
+    T *dC = st.mat(C, M, N, ldc, true);
+    l3::symm_simt<T>(left, Uplo == kUpper, M, N, alpha, dA, lda, dB, ldb, beta, dC, ldc);
+    st.finish();
+  });
+}
+
+// test/level3/syrk/exo_syrk_wrapper.h:9-28
+template <typename T>
+static void syrk_entry(const char *fn, int Order, int Uplo, int Trans, int N, int K, T alpha, const T *A, int lda,
+                       T beta, T *C, int ldc) {
+  guarded(fn, [&] {
+    row_major(Order);
+    nonneg(N, "N < 0");
+    nonneg(K, "K < 0");
+    if (N == 0) return;
+    const bool trans = Trans != kNoTrans;
+    const long ar = trans ? K : N, ac = trans ? N : K;
+    if (K > 0) ld_ok(lda, ac, "lda too small");
+    ld_ok(ldc, N, "ldc < max(1, N)");
+    Stager st;
+    const T *dA = K > 0 ? st.mat(A, ar, ac, lda, false) : A;
+    T *dC = st.mat(C, N, N, ldc, true);
+    l3::syrk_simt<T>(Uplo == kUpper, trans, N, K, alpha, dA, lda, beta, dC, ldc);
+    st.finish();
+  });
+}
+
+}  // namespace exb
+
+using namespace exb;
+
+extern "C" {
+
+void exo_sgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N,
+               const float alpha, const float *A, const int lda, const float *X, const int incX, const float beta,
+               float *Y, const int incY) {
+  gemv_entry<float>("exo_sgemv", order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_dgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N,
+               const double alpha, const double *A, const int lda, const double *X, const int incX, const double beta,
+               double *Y, const int incY) {
+  gemv_entry<double>("exo_dgemv", order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_sger(const enum CBLAS_ORDER order, const int M, const int N, const float alpha, const float *X,
+              const int incX, const float *Y, const int incY, float *A, const int lda) {
+  (void)order;
+  ger_entry<float>("exo_sger", M, N, alpha, X, incX, Y, incY, A, lda);
+}
+void exo_dger(const enum CBLAS_ORDER order, const int M, const int N, const double alpha, const double *X,
+              const int incX, const double *Y, const int incY, double *A, const int lda) {
+  (void)order;
+  ger_entry<double>("exo_dger", M, N, alpha, X, incX, Y, incY, A, lda);
+}
+void exo_ssymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
+               const float *A, const int lda, const float *X, const int incX, const float beta, float *Y,
+               const int incY) {
+  symv_entry<float>("exo_ssymv", order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_dsymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
+               const double *A, const int lda, const double *X, const int incX, const double beta, double *Y,
+               const int incY) {
+  symv_entry<double>("exo_dsymv", order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_ssyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
+              const float *X, const int incX, float *A, const int lda) {
+  syr_entry<float>("exo_ssyr", order, Uplo, N, alpha, X, incX, A, lda);
+}
+void exo_dsyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
+              const double *X, const int incX, double *A, const int lda) {
+  syr_entry<double>("exo_dsyr", order, Uplo, N, alpha, X, incX, A, lda);
+}
+void exo_ssyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
+               const float *X, const int incX, const float *Y, const int incY, float *A, const int lda) {
+  (void)order;
+  syr2_entry<float>("exo_ssyr2", Uplo, N, alpha, X, incX, Y, incY, A, lda);
+}
+void exo_dsyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
+               const double *X, const int incX, const double *Y, const int incY, double *A, const int lda) {
+  (void)order;
+  syr2_entry<double>("exo_dsyr2", Uplo, N, alpha, X, incX, Y, incY, A, lda);
+}
+void exo_strmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX) {
+  tr_entry<float, false>("exo_strmv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
+}
+void exo_dtrmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX) {
+  tr_entry<double, false>("exo_dtrmv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
+}
+void exo_strsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX) {
+  tr_entry<float, true>("exo_strsv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
+}
+void exo_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX) {
+  tr_entry<double, true>("exo_dtrsv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
+}
+
+void exo_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
+               const int M, const int N, const int K, const float alpha, const float *A, const int lda,
+               const float *B, const int ldb, const float beta, float *C, const int ldc) {
+  gemm_entry<float>("exo_sgemm", Order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_dgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
+               const int M, const int N, const int K, const double alpha, const double *A, const int lda,
+               const double *B, const int ldb, const double beta, double *C, const int ldc) {
+  gemm_entry<double>("exo_dgemm", Order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_ssymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
+               const int N, const float alpha, const float *A, const int lda, const float *B, const int ldb,
+               const float beta, float *C, const int ldc) {
+  symm_entry<float>("exo_ssymm", Order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_dsymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
+               const int N, const double alpha, const double *A, const int lda, const double *B, const int ldb,
+               const double beta, double *C, const int ldc) {
+  symm_entry<double>("exo_dsymm", Order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+               const int N, const int K, const float alpha, const float *A, const int lda, const float beta, float *C,
+               const int ldc) {
+  syrk_entry<float>("exo_ssyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+               const int N, const int K, const double alpha, const double *A, const int lda, const double beta,
+               double *C, const int ldc) {
+  syrk_entry<double>("exo_dsyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+// Plain-precision level 3 on the CUDA cores: FP32 FFMA (sgemm, ssymm, ssyrk)
+// and FP64 DFMA (dgemm, dsymm, dsyrk).  One tiled kernel template, with
+// operand loaders that express op(A)/op(B) (gemm), the symmetric operand
+// rebuilt from its stored triangle on load (symm) and A A^T / A^T A on the
+// triangle's tiles only (syrk).  beta is applied in the epilogue, fused with
+// the store, replacing the reference's separate mscal / trmscal pass
+// (test/level3/*/exo_*_wrapper.h, src/level3/mscal.py:12-28); it is applied
+// as a multiplication even when beta == 0, as that pass does.
+// Reference algorithms: src/level3/{gemm,symm,syrk}.py.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace exb {
+namespace l3 {
+
+// Operand views: element (r, c) of the logical operand.
+template <typename T>
+struct Plain {  // op(X) with op = transpose when t
+  const T *p;
+  long ld;
+  bool t;
+  __device__ __forceinline__ T operator()(long r, long c) const { return t ? p[c * ld + r] : p[r * ld + c]; }
+  __device__ __forceinline__ bool contiguous_cols() const { return !t; }
+};
+template <typename T>
+struct Sym {  // symmetric matrix from its stored triangle
+  const T *p;
+  long ld;
+  bool upper;
+  __device__ __forceinline__ T operator()(long r, long c) const {
+    const bool stored = upper ? (c >= r) : (c <= r);
+    return stored ? p[r * ld + c] : p[c * ld + r];
+  }
+  __device__ __forceinline__ bool contiguous_cols() const { return true; }
+};
+
+template <typename T>
+struct Cfg;
+template <>
+struct Cfg<float> {
+  static constexpr int BM = 128, BN = 128, BK = 16, TM = 8, TN = 8, THREADS = 256;
+};
+template <>
+struct Cfg<double> {
+  static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4, THREADS = 256;
+};
+
+// C tile (bm, bn) of rows m x cols n.  tri: 0 all tiles, 1 lower, 2 upper
+// (syrk): tiles strictly outside the triangle are not launched and elements
+// outside it are left untouched.
+template <typename T, class OA, class OB>
+__global__ void __launch_bounds__(Cfg<T>::THREADS)
+    gemm_kernel(long m, long n, long k, T alpha, OA opA, OB opB, T beta, T *C, long ldc, int tri) {
+  constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN, BK = Cfg<T>::BK, TM = Cfg<T>::TM, TN = Cfg<T>::TN;
+  constexpr int NT = Cfg<T>::THREADS;
+  constexpr int LA = BM * BK / NT, LB = BN * BK / NT;  // loads per thread per tile
+  constexpr int TX = BN / TN;                           // threads along n
+  __shared__ T As[2][BK][BM + 4];
+  __shared__ T Bs[2][BK][BN + 4];
+
+  long bm, bn;
+  if (tri == 0) {
+    bm = blockIdx.y;
+    bn = blockIdx.x;
+  } else {
+    // linear index over the lower triangle of tiles (bn <= bm); upper swaps
+    const long t = blockIdx.x;
+    long r = long((sqrt(8.0 * double(t) + 1.0) - 1.0) * 0.5);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    const long c = t - r * (r + 1) / 2;
+    bm = tri == 1 ? r : c;
+    bn = tri == 1 ? c : r;
+  }
+  const long row0 = bm * BM, col0 = bn * BN;
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+
+  const bool a_kfast = opA.contiguous_cols();  // A(i, k) contiguous along k
+  const bool b_nfast = opB.contiguous_cols();  // B(k, j) contiguous along j
+
+  T ra[LA], rb[LB];
+  auto fetch = [&](long k0) {
+#pragma unroll
+    for (int s = 0; s < LA; ++s) {
+      const int e = tid + s * NT;
+      const int i = a_kfast ? e / BK : e % BM, kk = a_kfast ? e % BK : e / BM;
+      const long gi = row0 + i, gk = k0 + kk;
+      ra[s] = (gi < m && gk < k) ? opA(gi, gk) : T(0);
+    }
+#pragma unroll
+    for (int s = 0; s < LB; ++s) {
+      const int e = tid + s * NT;
+      const int j = b_nfast ? e % BN : e / BK, kk = b_nfast ? e / BN : e % BK;
+      const long gj = col0 + j, gk = k0 + kk;
+      rb[s] = (gj < n && gk < k) ? opB(gk, gj) : T(0);
+    }
+  };
+  auto stash = [&](int buf) {
+#pragma unroll
+    for (int s = 0; s < LA; ++s) {
+      const int e = tid + s * NT;
+      const int i = a_kfast ? e / BK : e % BM, kk = a_kfast ? e % BK : e / BM;
+      As[buf][kk][i] = ra[s];
+    }
+#pragma unroll
+    for (int s = 0; s < LB; ++s) {
+      const int e = tid + s * NT;
+      const int j = b_nfast ? e % BN : e / BK, kk = b_nfast ? e / BN : e % BK;
+      Bs[buf][kk][j] = rb[s];
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int a = 0; a < TM; ++a)
+#pragma unroll
+    for (int b = 0; b < TN; ++b) acc[a][b] = 0;
+
+  const long ktiles = ceil_div(k, BK);
+  if (ktiles > 0) {
+    fetch(0);
+    stash(0);
+  }
+  __syncthreads();
+  for (long kt = 0; kt < ktiles; ++kt) {
+    const int buf = int(kt & 1);
+    if (kt + 1 < ktiles) fetch((kt + 1) * BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      T av[TM], bv[TN];
+      // rows ty*TM/2 .. and BM/2 + ty*TM/2 ..; cols likewise (conflict-free)
+#pragma unroll
+      for (int a = 0; a < TM / 2; ++a) {
+        av[a] = As[buf][kk][ty * (TM / 2) + a];
+        av[a + TM / 2] = As[buf][kk][BM / 2 + ty * (TM / 2) + a];
+      }
+#pragma unroll
+      for (int b = 0; b < TN / 2; ++b) {
+        bv[b] = Bs[buf][kk][tx * (TN / 2) + b];
+        bv[b + TN / 2] = Bs[buf][kk][BN / 2 + tx * (TN / 2) + b];
+      }
+#pragma unroll
+      for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+    }
+    if (kt + 1 < ktiles) stash(buf ^ 1);
+    __syncthreads();
+  }
+
+#pragma unroll
+  for (int a = 0; a < TM; ++a) {
+    const long gi = row0 + (a < TM / 2 ? ty * (TM / 2) + a : BM / 2 + ty * (TM / 2) + a - TM / 2);
+    if (gi >= m) continue;
+#pragma unroll
+    for (int b = 0; b < TN; ++b) {
+      const long gj = col0 + (b < TN / 2 ? tx * (TN / 2) + b : BN / 2 + tx * (TN / 2) + b - TN / 2);
+      if (gj >= n) continue;
+      if (tri == 1 && gj > gi) continue;
+      if (tri == 2 && gj < gi) continue;
+      T *c = C + gi * ldc + gj;
+      *c = alpha * acc[a][b] + beta * *c;
+    }
+  }
+}
+
+template <typename T, class OA, class OB>
+static void launch(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int tri) {
+  constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN;
+  if (m <= 0 || n <= 0) return;
+  dim3 grid;
+  if (tri == 0) {
+    grid = dim3(unsigned(ceil_div(n, BN)), unsigned(ceil_div(m, BM)));
+  } else {
+    const long nt = ceil_div(n, BM);  // BM == BN for every configuration
+    grid = dim3(unsigned(nt * (nt + 1) / 2));
+  }
+  gemm_kernel<T, OA, OB><<<grid, Cfg<T>::THREADS, 0, ctx().stream>>>(m, n, k, alpha, a, b, beta, C, ldc, tri);
+  EXB_LAUNCH("gemm kernel");
+  count_launch();
+}
+
+// src/level3/gemm.py:17-47 with the wrapper's beta pre-pass fused
+template <typename T>
+void gemm_simt(bool ta, bool tb, long m, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+               T *C, long ldc) {
+  launch<T>(m, n, k, alpha, Plain<T>{A, lda, ta}, Plain<T>{B, ldb, tb}, beta, C, ldc, 0);
+}
+
+// src/level3/symm.py:16-47
+template <typename T>
+void symm_simt(bool left, bool upper, long m, long n, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+               T *C, long ldc) {
+  if (left)
+    launch<T>(m, n, m, alpha, Sym<T>{A, lda, upper}, Plain<T>{B, ldb, false}, beta, C, ldc, 0);
+  else
+    launch<T>(m, n, n, alpha, Plain<T>{B, ldb, false}, Sym<T>{A, lda, upper}, beta, C, ldc, 0);
+}
+
+// src/level3/syrk.py:17-32: C_tri = alpha * op(A) op(A)^T + beta * C_tri
+template <typename T>
+void syrk_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, T beta, T *C, long ldc) {
+  // op(A) is n x k: NoTrans A[i,k]; Trans A^T[i,k] = A[k,i].  B = op(A)^T.
+  launch<T>(n, n, k, alpha, Plain<T>{A, lda, trans}, Plain<T>{A, lda, !trans}, beta, C, ldc, upper ? 2 : 1);
+}
+
+template void gemm_simt<float>(bool, bool, long, long, long, float, const float *, long, const float *, long, float,
+                               float *, long);
+template void gemm_simt<double>(bool, bool, long, long, long, double, const double *, long, const double *, long,
+                                double, double *, long);
+template void symm_simt<float>(bool, bool, long, long, float, const float *, long, const float *, long, float, float *,
+                               long);
+template void symm_simt<double>(bool, bool, long, long, double, const double *, long, const double *, long, double,
+                                double *, long);
+template void syrk_simt<float>(bool, bool, long, long, float, const float *, long, float, float *, long);
+template void syrk_simt<double>(bool, bool, long, long, double, const double *, long, double, double *, long);
+
+}  // namespace l3
+}  // namespace exb

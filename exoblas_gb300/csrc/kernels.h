@@ -1,0 +1,65 @@
+// Launchers for the device kernels.  All pointers are device pointers; vector
+// element i lives at p[i * inc] (inc may be negative, the pointer already
+// rebased to element 0 exactly as the reference wrappers do).  Launchers
+// enqueue on ctx().stream and never synchronise.
+#pragma once
+
+#include "common.cuh"
+
+namespace exb {
+
+namespace l1 {
+template <typename T>
+void axpy(long n, T alpha, const T *x, long incx, T *y, long incy);
+template <typename T>
+void scal(long n, T alpha, T *x, long incx);  // alpha == 0 writes zeros
+template <typename T>
+void copy(long n, const T *x, long incx, T *y, long incy);
+template <typename T>
+void swap(long n, T *x, long incx, T *y, long incy);
+template <typename T>
+void rot(long n, T *x, long incx, T *y, long incy, T c, T s);
+// P[0] is the flag (-1, 0, 1 act; anything else is a no-op); P on the host
+template <typename T>
+void rotm(long n, T *x, long incx, T *y, long incy, const T P[5]);
+template <typename T>
+void asum(long n, const T *x, long incx, T *result);
+template <typename T>
+void dot(long n, const T *x, long incx, const T *y, long incy, T *result);
+// result (double) = sum of double(x_i) * double(y_i); if sresult != nullptr
+// also writes float(result + sb) there (sdsdot)
+void dsdot(long n, const float *x, long incx, const float *y, long incy, double *result, float sb, float *sresult);
+}  // namespace l1
+
+namespace l2 {
+// y = beta*y + alpha*op(A) x; A row-major rows x cols (the caller's M x N)
+template <typename T>
+void gemv(bool trans, long rows, long cols, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y,
+          long incy);
+template <typename T>
+void ger(long m, long n, T alpha, const T *x, long incx, const T *y, long incy, T *A, long lda);
+template <typename T>
+void symv(bool upper, long n, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y, long incy);
+template <typename T>
+void syr(bool upper, long n, T alpha, const T *x, long incx, T *A, long lda);
+template <typename T>
+void syr2(bool upper, long n, T alpha, const T *x, long incx, const T *y, long incy, T *A, long lda);
+template <typename T>
+void trmv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx);
+template <typename T>
+void trsv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx);
+}  // namespace l2
+
+namespace l3 {
+// CUDA-core (FFMA / DFMA) paths
+template <typename T>
+void gemm_simt(bool ta, bool tb, long m, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+               T *C, long ldc);
+template <typename T>
+void symm_simt(bool left, bool upper, long m, long n, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+               T *C, long ldc);
+template <typename T>
+void syrk_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, T beta, T *C, long ldc);
+}  // namespace l3
+
+}  // namespace exb

@@ -1,0 +1,532 @@
+// Level-2 kernels (gemv, ger, symv, syr, syr2, trmv): each streams the
+// matrix from HBM once with 16-byte loads.  Reductions across CTAs go
+// through per-chunk partial rows in scratch that a second kernel sums in a
+// fixed order, so results are deterministic.
+// Reference algorithms: src/level2/{gemv,ger,symv,syr,syr2,trmv}.py.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace exb {
+namespace l2 {
+
+constexpr int kThreads = 256;
+
+// Carves one scratch allocation into 256-byte aligned regions.
+struct Carve {
+  size_t off = 0;
+  char *base = nullptr;
+  template <typename T>
+  size_t add(long n) {
+    size_t o = off;
+    off += (size_t(n > 0 ? n : 1) * sizeof(T) + 255) & ~size_t(255);
+    return o;
+  }
+  void alloc() { base = static_cast<char *>(scratch(off)); }
+  template <typename T>
+  T *at(size_t o) const {
+    return reinterpret_cast<T *>(base + o);
+  }
+};
+
+template <typename T>
+static bool vec_ok(const T *A, long lda) {
+  return aligned16(A) && (lda * long(sizeof(T))) % 16 == 0;
+}
+
+// Contiguous copy of a strided vector (element i of src at src[i*inc]).
+template <typename T>
+__global__ void pack_kernel(long n, const T *__restrict__ src, long inc, T *__restrict__ dst) {
+  for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
+    dst[i] = src[i * inc];
+}
+template <typename T>
+static void pack(long n, const T *src, long inc, T *dst) {
+  if (n <= 0) return;
+  long blocks = ceil_div(n, kThreads);
+  if (blocks > grid_cap(4)) blocks = grid_cap(4);
+  pack_kernel<T><<<int(blocks), kThreads, 0, ctx().stream>>>(n, src, inc, dst);
+  EXB_LAUNCH("pack kernel");
+  count_launch();
+}
+
+// Returns a unit-stride, 16-byte aligned view of x (packing into `tmp` when needed).
+template <typename T>
+static const T *unit_view(long n, const T *x, long inc, T *tmp) {
+  if (inc == 1 && aligned16(x)) return x;
+  pack(n, x, inc, tmp);
+  return tmp;
+}
+
+// ------------------------------------------------------------ row dots ----
+// out_i = sum_{j in [lo(i), hi(i))} A[i,j] * x[j] for every row i, G threads
+// per row.  MODE 0 (gemv N): y_i = alpha*dot + beta*y_i.  MODE 1 (trmv N):
+// x_i = dot (+ xs_i for a unit diagonal, the diagonal being excluded from
+// the range).  `tri`: 0 full row, 1 lower (j <= i), 2 upper (j >= i).
+template <typename T, int G, bool VEC, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    rowdot_kernel(long rows, long cols, T alpha, const T *__restrict__ A, long lda, const T *__restrict__ x, T beta,
+                  T *y, long incy, int tri, bool unit) {
+  using V = typename V16<T>::type;
+  constexpr int VN = V16<T>::N;
+  constexpr int RPW = 32 / G;  // rows per warp
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % G;
+  const long warp_global = (long(blockIdx.x) * kThreads + threadIdx.x) / 32;
+  const long nwarps = long(gridDim.x) * (kThreads / 32);
+  for (long base = warp_global * RPW; base < rows; base += nwarps * RPW) {
+    const long i = base + lane / G;
+    T acc = 0;
+    if (i < rows) {
+      long lo = 0, hi = cols;
+      if (tri == 1) hi = (unit ? i : i + 1);
+      else if (tri == 2) lo = (unit ? i + 1 : i);
+      if (hi > cols) hi = cols;
+      const T *a = A + i * lda;
+      if (VEC && hi - lo >= VN) {
+        // scalar head up to a 16-byte boundary, then vectors, then a scalar tail
+        const long vlo = (lo + VN - 1) / VN * VN, vhi = hi / VN * VN;
+        for (long j = lo + sub; j < vlo && j < hi; j += G) acc = fma(a[j], x[j], acc);
+        const V *av = reinterpret_cast<const V *>(a);
+        const V *xv = reinterpret_cast<const V *>(x);
+        long v = vlo / VN + sub;
+        const long ve = vhi / VN;
+        for (; v + 3 * G < ve; v += 4 * G) {
+          V a0 = ld_stream(av + v), a1 = ld_stream(av + v + G), a2 = ld_stream(av + v + 2 * G),
+            a3 = ld_stream(av + v + 3 * G);
+          V x0 = xv[v], x1 = xv[v + G], x2 = xv[v + 2 * G], x3 = xv[v + 3 * G];
+#pragma unroll
+          for (int e = 0; e < VN; ++e) {
+            acc = fma(vget<T>(a0, e), vget<T>(x0, e), acc);
+            acc = fma(vget<T>(a1, e), vget<T>(x1, e), acc);
+            acc = fma(vget<T>(a2, e), vget<T>(x2, e), acc);
+            acc = fma(vget<T>(a3, e), vget<T>(x3, e), acc);
+          }
+        }
+        for (; v < ve; v += G) {
+          V a0 = ld_stream(av + v), x0 = xv[v];
+#pragma unroll
+          for (int e = 0; e < VN; ++e) acc = fma(vget<T>(a0, e), vget<T>(x0, e), acc);
+        }
+        for (long j = (vhi > vlo ? vhi : vlo) + sub; j < hi; j += G) acc = fma(a[j], x[j], acc);
+      } else {
+        for (long j = lo + sub; j < hi; j += G) acc = fma(a[j], x[j], acc);
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (i < rows && sub == 0) {
+      if (MODE == 0) {
+        T *yi = y + i * incy;
+        *yi = alpha * acc + beta * *yi;
+      } else {
+        y[i * incy] = unit ? acc + x[i] : acc;
+      }
+    }
+  }
+}
+
+template <typename T, int MODE>
+static void launch_rowdot(long rows, long cols, T alpha, const T *A, long lda, const T *xu, T beta, T *y, long incy,
+                          int tri, bool unit) {
+  cudaStream_t s = ctx().stream;
+  const bool vec = vec_ok(A, lda) && aligned16(xu);
+  const int G = cols >= 256 ? 32 : 4;
+  const long rpb = (kThreads / 32) * (32 / G);
+  long blocks = ceil_div(rows, rpb);
+  if (blocks > grid_cap(16)) blocks = grid_cap(16);
+  if (blocks < 1) blocks = 1;
+#define EXB_ROWDOT(GG, VV) \
+  rowdot_kernel<T, GG, VV, MODE><<<int(blocks), kThreads, 0, s>>>(rows, cols, alpha, A, lda, xu, beta, y, incy, tri, unit)
+  if (G == 32) {
+    if (vec) EXB_ROWDOT(32, true);
+    else EXB_ROWDOT(32, false);
+  } else {
+    if (vec) EXB_ROWDOT(4, true);
+    else EXB_ROWDOT(4, false);
+  }
+#undef EXB_ROWDOT
+  EXB_LAUNCH("row-dot kernel");
+  count_launch();
+}
+
+// ------------------------------------------------------------ column sums --
+// partial[c][j] = sum over rows i of chunk c of A[i,j] * x[i] (restricted to
+// the triangle when tri != 0).  A warp covers 32*VN columns; the 8 warps of
+// a CTA take interleaved rows of the chunk and are summed in warp order.
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kThreads)
+    colsum_kernel(long rows, long cols, const T *__restrict__ A, long lda, const T *__restrict__ x, long rows_per_chunk,
+                  T *__restrict__ partial, int tri, bool unit) {
+  using V = typename V16<T>::type;
+  constexpr int VN = V16<T>::N;
+  __shared__ T sh[kThreads / 32][32 * VN];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long j0 = long(blockIdx.x) * 32 * VN + lane * VN;
+  const long r0 = long(blockIdx.y) * rows_per_chunk;
+  long r1 = r0 + rows_per_chunk;
+  if (r1 > rows) r1 = rows;
+  T acc[VN];
+#pragma unroll
+  for (int e = 0; e < VN; ++e) acc[e] = 0;
+  // rows of the triangle that can touch columns [j0, j0+VN)
+  long rlo = r0, rhi = r1;
+  if (tri == 1 && rlo < j0) rlo = j0;                       // lower: i >= j
+  if (tri == 2 && rhi > j0 + VN) rhi = j0 + VN;             // upper: i <= j
+  const bool full_vec = VEC && j0 + VN <= cols;
+  long i = rlo + warp;
+  if (full_vec && tri == 0) {
+    for (; i + 3 * 8 < rhi; i += 4 * 8) {
+      V a0 = ld_stream(reinterpret_cast<const V *>(A + i * lda + j0));
+      V a1 = ld_stream(reinterpret_cast<const V *>(A + (i + 8) * lda + j0));
+      V a2 = ld_stream(reinterpret_cast<const V *>(A + (i + 16) * lda + j0));
+      V a3 = ld_stream(reinterpret_cast<const V *>(A + (i + 24) * lda + j0));
+      const T x0 = x[i], x1 = x[i + 8], x2 = x[i + 16], x3 = x[i + 24];
+#pragma unroll
+      for (int e = 0; e < VN; ++e) {
+        acc[e] = fma(vget<T>(a0, e), x0, acc[e]);
+        acc[e] = fma(vget<T>(a1, e), x1, acc[e]);
+        acc[e] = fma(vget<T>(a2, e), x2, acc[e]);
+        acc[e] = fma(vget<T>(a3, e), x3, acc[e]);
+      }
+    }
+  }
+  for (; i < rhi; i += 8) {
+    const T xi = x[i];
+    if (full_vec) {
+      V a = ld_stream(reinterpret_cast<const V *>(A + i * lda + j0));
+#pragma unroll
+      for (int e = 0; e < VN; ++e) {
+        const long j = j0 + e;
+        const bool in = tri == 0 || (tri == 1 ? (unit ? j < i : j <= i) : (unit ? j > i : j >= i));
+        if (in) acc[e] = fma(vget<T>(a, e), xi, acc[e]);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < VN; ++e) {
+        const long j = j0 + e;
+        if (j >= cols) continue;
+        const bool in = tri == 0 || (tri == 1 ? (unit ? j < i : j <= i) : (unit ? j > i : j >= i));
+        if (in) acc[e] = fma(A[i * lda + j], xi, acc[e]);
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < VN; ++e) sh[warp][lane * VN + e] = acc[e];
+  __syncthreads();
+  for (int t = threadIdx.x; t < 32 * VN; t += kThreads) {
+    T s = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) s += sh[w][t];
+    const long j = long(blockIdx.x) * 32 * VN + t;
+    if (j < cols) partial[long(blockIdx.y) * cols + j] = s;
+  }
+}
+
+// MODE 0: y_j = alpha * sum_c partial[c][j] + beta * y_j (gemv T, symv)
+// MODE 1: y_j = sum_c partial[c][j] (+ xs_j when unit)  (trmv T)
+template <typename T, int MODE>
+__global__ void finish_kernel(long cols, int chunks, const T *__restrict__ partial, T alpha, T beta, T *y, long incy,
+                              const T *xs, bool unit) {
+  for (long j = long(blockIdx.x) * blockDim.x + threadIdx.x; j < cols; j += long(gridDim.x) * blockDim.x) {
+    T s = 0;
+    for (int c = 0; c < chunks; ++c) s += partial[long(c) * cols + j];
+    T *yj = y + j * incy;
+    if (MODE == 0)
+      *yj = alpha * s + beta * *yj;
+    else
+      *yj = unit ? s + xs[j] : s;
+  }
+}
+
+template <typename T>
+static int colsum_chunks(long rows, long cols) {
+  constexpr int VN = V16<T>::N;
+  const long tiles = ceil_div(cols, 32 * VN);
+  long chunks = ceil_div(grid_cap(4), tiles);
+  const long max_chunks = ceil_div(rows, 64);
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks < 1) chunks = 1;
+  return int(chunks);
+}
+
+template <typename T>
+static void launch_colsum(long rows, long cols, const T *A, long lda, const T *xu, int chunks, T *partial, int tri,
+                          bool unit) {
+  constexpr int VN = V16<T>::N;
+  const long rpc = ceil_div(rows, chunks);
+  dim3 grid(unsigned(ceil_div(cols, 32 * VN)), unsigned(chunks));
+  if (vec_ok(A, lda))
+    colsum_kernel<T, true><<<grid, kThreads, 0, ctx().stream>>>(rows, cols, A, lda, xu, rpc, partial, tri, unit);
+  else
+    colsum_kernel<T, false><<<grid, kThreads, 0, ctx().stream>>>(rows, cols, A, lda, xu, rpc, partial, tri, unit);
+  EXB_LAUNCH("column-sum kernel");
+  count_launch();
+}
+
+template <typename T, int MODE>
+static void launch_finish(long cols, int chunks, const T *partial, T alpha, T beta, T *y, long incy, const T *xs,
+                          bool unit) {
+  long blocks = ceil_div(cols, kThreads);
+  if (blocks > grid_cap(4)) blocks = grid_cap(4);
+  finish_kernel<T, MODE><<<int(blocks), kThreads, 0, ctx().stream>>>(cols, chunks, partial, alpha, beta, y, incy, xs,
+                                                                     unit);
+  EXB_LAUNCH("partial-sum kernel");
+  count_launch();
+}
+
+// src/level2/gemv.py:10-22.  rows x cols is the caller's M x N matrix.
+template <typename T>
+void gemv(bool trans, long rows, long cols, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y,
+          long incy) {
+  if (rows <= 0 && cols <= 0) return;
+  const long xlen = trans ? rows : cols, ylen = trans ? cols : rows;
+  if (ylen <= 0) return;
+  if (xlen <= 0) {
+    // y = beta * y (gemv.py:13-14) with nothing to add
+    l1::scal<T>(ylen, beta, y, incy);
+    return;
+  }
+  Carve cv;
+  const size_t ox = cv.add<T>(xlen);
+  const int chunks = trans ? colsum_chunks<T>(rows, cols) : 0;
+  const size_t op = trans ? cv.add<T>(long(chunks) * cols) : 0;
+  cv.alloc();
+  const T *xu = unit_view(xlen, x, incx, cv.at<T>(ox));
+  if (!trans) {
+    launch_rowdot<T, 0>(rows, cols, alpha, A, lda, xu, beta, y, incy, 0, false);
+  } else {
+    T *partial = cv.at<T>(op);
+    launch_colsum<T>(rows, cols, A, lda, xu, chunks, partial, 0, false);
+    launch_finish<T, 0>(cols, chunks, partial, alpha, beta, y, incy, nullptr, false);
+  }
+}
+
+// src/level2/trmv.py:9-43: x = op(A) x with A triangular.
+template <typename T>
+void trmv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx) {
+  if (n <= 0) return;
+  Carve cv;
+  const size_t ox = cv.add<T>(n);
+  const int chunks = trans ? colsum_chunks<T>(n, n) : 0;
+  const size_t op = trans ? cv.add<T>(long(chunks) * n) : 0;
+  cv.alloc();
+  T *xs = cv.at<T>(ox);
+  pack(n, x, incx, xs);  // the kernels read this copy; x is the output
+  const int tri = upper ? 2 : 1;
+  if (!trans) {
+    launch_rowdot<T, 1>(n, n, T(1), A, lda, xs, T(0), x, incx, tri, unit);
+  } else {
+    T *partial = cv.at<T>(op);
+    launch_colsum<T>(n, n, A, lda, xs, chunks, partial, tri, unit);
+    launch_finish<T, 1>(n, chunks, partial, T(1), T(0), x, incx, xs, unit);
+  }
+}
+
+// ---------------------------------------------------------- rank updates --
+// One CTA per row (grid-stride): the row's columns [lo, hi) are updated in
+// 16-byte vectors with scalar head/tail.  MODE 0 ger, 1 syr, 2 syr2.
+template <typename T, bool VEC, int MODE>
+__global__ void __launch_bounds__(kThreads)
+    rank_kernel(long rows, long cols, T alpha, const T *__restrict__ x, const T *__restrict__ y, T *A, long lda,
+                int tri) {
+  using V = typename V16<T>::type;
+  constexpr int VN = V16<T>::N;
+  for (long i = blockIdx.x; i < rows; i += gridDim.x) {
+    long lo = 0, hi = cols;
+    if (tri == 1) hi = i + 1;  // lower
+    if (tri == 2) lo = i;      // upper
+    T *a = A + i * lda;
+    const T ax = alpha * x[i];                  // ger.py:15, syr.py:17-19
+    const T ay = MODE == 2 ? alpha * y[i] : T(0);  // syr2.py:25-27
+    const T *u = MODE == 1 ? x : y;
+    auto upd = [&](T av, long j) -> T {
+      if (MODE == 2) return av + (ax * y[j] + ay * x[j]);
+      return av + ax * u[j];
+    };
+    if (VEC) {
+      const long vlo = (lo + VN - 1) / VN * VN, vhi = hi / VN * VN;
+      for (long j = lo + threadIdx.x; j < vlo && j < hi; j += kThreads) a[j] = upd(a[j], j);
+      V *av = reinterpret_cast<V *>(a);
+      for (long v = vlo / VN + threadIdx.x; v < vhi / VN; v += kThreads) {
+        V t = av[v];
+#pragma unroll
+        for (int e = 0; e < VN; ++e) vset<T>(t, e, upd(vget<T>(t, e), v * VN + e));
+        av[v] = t;
+      }
+      for (long j = (vhi > vlo ? vhi : vlo) + threadIdx.x; j < hi; j += kThreads) a[j] = upd(a[j], j);
+    } else {
+      for (long j = lo + threadIdx.x; j < hi; j += kThreads) a[j] = upd(a[j], j);
+    }
+  }
+}
+
+template <typename T, int MODE>
+static void launch_rank(long rows, long cols, T alpha, const T *xu, const T *yu, T *A, long lda, int tri) {
+  long blocks = rows;
+  if (blocks > grid_cap(8)) blocks = grid_cap(8);
+  if (vec_ok(A, lda))
+    rank_kernel<T, true, MODE><<<int(blocks), kThreads, 0, ctx().stream>>>(rows, cols, alpha, xu, yu, A, lda, tri);
+  else
+    rank_kernel<T, false, MODE><<<int(blocks), kThreads, 0, ctx().stream>>>(rows, cols, alpha, xu, yu, A, lda, tri);
+  EXB_LAUNCH("rank-update kernel");
+  count_launch();
+}
+
+// src/level2/ger.py:9-15
+template <typename T>
+void ger(long m, long n, T alpha, const T *x, long incx, const T *y, long incy, T *A, long lda) {
+  if (m <= 0 || n <= 0) return;
+  Carve cv;
+  const size_t ox = cv.add<T>(m), oy = cv.add<T>(n);
+  cv.alloc();
+  const T *xu = unit_view(m, x, incx, cv.at<T>(ox));
+  const T *yu = unit_view(n, y, incy, cv.at<T>(oy));
+  launch_rank<T, 0>(m, n, alpha, xu, yu, A, lda, 0);
+}
+
+// src/level2/syr.py:10-19
+template <typename T>
+void syr(bool upper, long n, T alpha, const T *x, long incx, T *A, long lda) {
+  if (n <= 0) return;
+  Carve cv;
+  const size_t ox = cv.add<T>(n);
+  cv.alloc();
+  const T *xu = unit_view(n, x, incx, cv.at<T>(ox));
+  launch_rank<T, 1>(n, n, alpha, xu, xu, A, lda, upper ? 2 : 1);
+}
+
+// src/level2/syr2.py:9-27
+template <typename T>
+void syr2(bool upper, long n, T alpha, const T *x, long incx, const T *y, long incy, T *A, long lda) {
+  if (n <= 0) return;
+  Carve cv;
+  const size_t ox = cv.add<T>(n), oy = cv.add<T>(n);
+  cv.alloc();
+  const T *xu = unit_view(n, x, incx, cv.at<T>(ox));
+  const T *yu = unit_view(n, y, incy, cv.at<T>(oy));
+  launch_rank<T, 2>(n, n, alpha, xu, yu, A, lda, upper ? 2 : 1);
+}
+
+// ------------------------------------------------------------------- symv --
+// src/level2/symv.py:10-35.  The stored triangle is cut into 64 x 64 tiles;
+// each CTA reads one tile once and produces both its row contribution
+// (A_t x_cols) and, for off-diagonal tiles, its column contribution
+// (A_t^T x_rows).  Output row tile r receives one contribution per tile index
+// c (slot c): P[c][rows of r].  A second kernel sums the slots in order.
+constexpr int kSymTile = 64;
+
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kThreads)
+    symv_tile_kernel(long n, const T *__restrict__ A, long lda, const T *__restrict__ x, T *__restrict__ P, bool upper) {
+  constexpr int VN = V16<T>::N;
+  constexpr int TPR = kSymTile / VN;       // threads per tile row (16 float, 32 double)
+  constexpr int RPP = kThreads / TPR;      // rows per pass
+  constexpr int PASSES = kSymTile / RPP;
+  using V = typename V16<T>::type;
+  __shared__ T colsh[RPP][kSymTile];
+  __shared__ T rowsh[kSymTile];
+  // tile index -> (bi, bj) of the lower triangle of tiles
+  const long k = blockIdx.x;
+  long bi = long((sqrt(8.0 * double(k) + 1.0) - 1.0) * 0.5);
+  while (bi * (bi + 1) / 2 > k) --bi;
+  while ((bi + 1) * (bi + 2) / 2 <= k) ++bi;
+  const long bj = k - bi * (bi + 1) / 2;
+  // stored tile: lower -> rows bi, cols bj; upper -> rows bj, cols bi
+  const long tr = upper ? bj : bi, tc = upper ? bi : bj;
+  const bool diag = bi == bj;
+  const int tx = threadIdx.x % TPR, ty = threadIdx.x / TPR;
+  const long c0 = tc * kSymTile + tx * VN;
+  T colacc[VN];
+#pragma unroll
+  for (int e = 0; e < VN; ++e) colacc[e] = 0;
+  T xc[VN];
+#pragma unroll
+  for (int e = 0; e < VN; ++e) xc[e] = c0 + e < n ? x[c0 + e] : T(0);
+#pragma unroll
+  for (int p = 0; p < PASSES; ++p) {
+    const int rr = p * RPP + ty;
+    const long r = tr * kSymTile + rr;
+    T av[VN];
+    if (r < n) {
+      const T *a = A + r * lda + c0;
+      if (VEC && c0 + VN <= n) {
+        V v = ld_stream(reinterpret_cast<const V *>(a));
+#pragma unroll
+        for (int e = 0; e < VN; ++e) av[e] = vget<T>(v, e);
+      } else {
+#pragma unroll
+        for (int e = 0; e < VN; ++e) av[e] = c0 + e < n ? a[e] : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int e = 0; e < VN; ++e) av[e] = 0;
+    }
+    const T xr = r < n ? x[r] : T(0);
+    T rowacc = 0;
+#pragma unroll
+    for (int e = 0; e < VN; ++e) {
+      const long c = c0 + e;
+      // stored-triangle membership inside a diagonal tile
+      const bool in_row = !diag || (upper ? c >= r : c <= r);
+      const bool in_col = !diag || (upper ? c > r : c < r);
+      const T a = (r < n && c < n) ? av[e] : T(0);
+      if (in_row) rowacc = fma(a, xc[e], rowacc);
+      if (in_col) colacc[e] = fma(a, xr, colacc[e]);
+    }
+#pragma unroll
+    for (int o = TPR / 2; o > 0; o >>= 1) rowacc += __shfl_xor_sync(0xffffffffu, rowacc, o);
+    if (tx == 0) rowsh[rr] = rowacc;
+  }
+#pragma unroll
+  for (int e = 0; e < VN; ++e) colsh[ty][tx * VN + e] = colacc[e];
+  __syncthreads();
+  if (threadIdx.x < kSymTile) {
+    const int t = threadIdx.x;
+    T cs = 0;
+#pragma unroll 4
+    for (int q = 0; q < RPP; ++q) cs += colsh[q][t];
+    const long rrow = tr * kSymTile + t;  // output rows of the stored tile's rows
+    const long rcol = tc * kSymTile + t;  // output rows of the stored tile's cols
+    if (diag) {
+      if (rrow < n) P[tc * n + rrow] = rowsh[t] + cs;
+    } else {
+      if (rrow < n) P[tc * n + rrow] = rowsh[t];
+      if (rcol < n) P[tr * n + rcol] = cs;
+    }
+  }
+}
+
+template <typename T>
+void symv(bool upper, long n, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y, long incy) {
+  if (n <= 0) return;
+  const long nt = ceil_div(n, kSymTile);
+  Carve cv;
+  const size_t ox = cv.add<T>(n), op = cv.add<T>(nt * n);
+  cv.alloc();
+  const T *xu = unit_view(n, x, incx, cv.at<T>(ox));
+  T *P = cv.at<T>(op);
+  const long tiles = nt * (nt + 1) / 2;
+  if (vec_ok(A, lda))
+    symv_tile_kernel<T, true><<<unsigned(tiles), kThreads, 0, ctx().stream>>>(n, A, lda, xu, P, upper);
+  else
+    symv_tile_kernel<T, false><<<unsigned(tiles), kThreads, 0, ctx().stream>>>(n, A, lda, xu, P, upper);
+  EXB_LAUNCH("symv tile kernel");
+  count_launch();
+  launch_finish<T, 0>(n, int(nt), P, alpha, beta, y, incy, nullptr, false);
+}
+
+#define EXB_L2_INST(T)                                                                                   \
+  template void gemv<T>(bool, long, long, T, const T *, long, const T *, long, T, T *, long);            \
+  template void trmv<T>(bool, bool, bool, long, const T *, long, T *, long);                             \
+  template void ger<T>(long, long, T, const T *, long, const T *, long, T *, long);                      \
+  template void syr<T>(bool, long, T, const T *, long, T *, long);                                       \
+  template void syr2<T>(bool, long, T, const T *, long, const T *, long, T *, long);                     \
+  template void symv<T>(bool, long, T, const T *, long, const T *, long, T, T *, long);
+EXB_L2_INST(float)
+EXB_L2_INST(double)
+
+}  // namespace l2
+}  // namespace exb

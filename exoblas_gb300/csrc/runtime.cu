@@ -1,0 +1,279 @@
+// Per-thread execution state, workspace arenas, status reporting and the
+// host-operand staging used by every exo_* entry point.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+#include "runtime.h"
+
+namespace exb {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static thread_local int tl_status = EXOBLAS_SUCCESS;
+static exoblas_error_handler g_handler = nullptr;
+
+void fail(int status, const char *what) { throw Error{status, what}; }
+
+void check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return;
+  static thread_local char buf[512];
+  snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) throw Error{EXOBLAS_ALLOC_FAILED, buf};
+  throw Error{EXOBLAS_CUDA_ERROR, buf};
+}
+
+void *Arena::get(size_t need) {
+  if (need == 0) need = 256;
+  if (need <= bytes) return ptr;
+  if (ptr) {
+    // the previous buffer may still be read by queued work of this thread
+    cudaStreamSynchronize(ctx().stream);
+    cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  size_t want = need + need / 4;
+  want = (want + 0xFFFFF) & ~size_t(0xFFFFF);  // whole MiB
+  cudaError_t e = cudaMalloc(&ptr, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(&ptr, need);
+    want = need;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ptr = nullptr;
+    fail(EXOBLAS_ALLOC_FAILED, "device workspace allocation failed");
+  }
+  bytes = want;
+  return ptr;
+}
+
+void Arena::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+Context::~Context() {
+  // Runs at thread exit; the CUDA runtime may already be shutting down at
+  // process exit, so errors are ignored.
+  scratch.release();
+  counters.release();
+  for (auto &s : staging) s.release();
+  if (own_stream && stream) cudaStreamDestroy(stream);
+  cudaGetLastError();
+}
+
+static int initial_precision() {
+  const char *e = getenv("EXOBLAS_PRECISION_MODE");
+  if (!e) return EXOBLAS_PRECISION_NATIVE;
+  if (!strcmp(e, "split_bf16")) return EXOBLAS_PRECISION_SPLIT_BF16;
+  if (!strcmp(e, "ozaki")) return EXOBLAS_PRECISION_OZAKI;
+  return EXOBLAS_PRECISION_NATIVE;
+}
+
+constexpr int kMaxDevices = 64;
+static thread_local Context *tl_ctx[kMaxDevices] = {};
+struct CtxOwner {
+  ~CtxOwner() {
+    for (auto &c : tl_ctx) {
+      delete c;
+      c = nullptr;
+    }
+  }
+};
+static thread_local CtxOwner tl_owner;
+
+Context &ctx() {
+  int dev = 0;
+  EXB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) fail(EXOBLAS_NOT_SUPPORTED, "device index out of range");
+  Context *&c = tl_ctx[dev];
+  if (!c) {
+    (void)&tl_owner;
+    Context *n = new Context();
+    n->device = dev;
+    n->precision = initial_precision();
+    cudaDeviceProp prop;
+    EXB_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (prop.major < 10) {
+      delete n;
+      fail(EXOBLAS_NOT_SUPPORTED, "libexoblas_gb300 requires a Blackwell (sm_103) device");
+    }
+    n->sm_count = prop.multiProcessorCount;
+    EXB_CUDA(cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking));
+    n->own_stream = true;
+    c = n;
+  }
+  return *c;
+}
+
+void *scratch(size_t bytes) { return ctx().scratch.get((bytes + 255) & ~size_t(255)); }
+
+unsigned int *zero_words(int n) {
+  Context &c = ctx();
+  const size_t need = size_t(n) * 4;
+  if (c.counters.bytes < need) {
+    c.counters.get(need < 4096 ? 4096 : need);
+    EXB_CUDA(cudaMemsetAsync(c.counters.ptr, 0, c.counters.bytes, c.stream));
+  }
+  return static_cast<unsigned int *>(c.counters.ptr);
+}
+
+// ---------------------------------------------------------------- staging --
+
+bool is_device_pointer(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+Stager::Stager() : c(ctx()) {}
+
+void *Stager::stage(const void *p, size_t elem, long count, long inc, bool out) {
+  // Span of a strided vector whose element 0 is at p and element i at p + i*inc
+  if (count <= 0 || !p) return const_cast<void *>(p);
+  if (is_device_pointer(p)) return const_cast<void *>(p);
+  const long lo = inc < 0 ? (count - 1) * inc : 0;
+  const long hi = inc < 0 ? 0 : (count - 1) * inc;
+  const size_t bytes = size_t(hi - lo + 1) * elem;
+  const char *base = static_cast<const char *>(p) + lo * long(elem);
+  if (nslots >= kSlots) fail(EXOBLAS_INVALID_VALUE, "too many host operands");
+  char *d = static_cast<char *>(c.staging[nslots].get(bytes));
+  EXB_CUDA(cudaMemcpyAsync(d, base, bytes, cudaMemcpyHostToDevice, c.stream));
+  Slot &s = slots[nslots++];
+  s = Slot{const_cast<char *>(base), d, bytes, 0, 0, 0, out};
+  any_host = true;
+  h2d += bytes;
+  return d - lo * long(elem);
+}
+
+void *Stager::stage_matrix(const void *p, size_t elem, long rows, long cols, long ld, bool out) {
+  if (rows <= 0 || cols <= 0 || !p) return const_cast<void *>(p);
+  if (is_device_pointer(p)) return const_cast<void *>(p);
+  const size_t bytes = size_t((rows - 1) * ld + cols) * elem;
+  if (nslots >= kSlots) fail(EXOBLAS_INVALID_VALUE, "too many host operands");
+  char *d = static_cast<char *>(c.staging[nslots].get(bytes));
+  const size_t pitch = size_t(ld) * elem, width = size_t(cols) * elem;
+  if (ld == cols)
+    EXB_CUDA(cudaMemcpyAsync(d, p, bytes, cudaMemcpyHostToDevice, c.stream));
+  else
+    EXB_CUDA(cudaMemcpy2DAsync(d, pitch, p, pitch, width, rows, cudaMemcpyHostToDevice, c.stream));
+  Slot &s = slots[nslots++];
+  s = Slot{const_cast<void *>(p), d, bytes, pitch, width, size_t(rows), out};
+  any_host = true;
+  h2d += size_t(rows) * width;
+  return d;
+}
+
+void Stager::finish() {
+  for (int i = 0; i < nslots; ++i) {
+    Slot &s = slots[i];
+    if (!s.out) continue;
+    if (s.rows) {
+      // matrices: copy back only the rows' used columns so padding between
+      // rows (ld > cols) is never written
+      if (s.pitch == s.width)
+        EXB_CUDA(cudaMemcpyAsync(s.host, s.dev, s.bytes, cudaMemcpyDeviceToHost, c.stream));
+      else
+        EXB_CUDA(cudaMemcpy2DAsync(s.host, s.pitch, s.dev, s.pitch, s.width, s.rows, cudaMemcpyDeviceToHost,
+                                   c.stream));
+    } else {
+      EXB_CUDA(cudaMemcpyAsync(s.host, s.dev, s.bytes, cudaMemcpyDeviceToHost, c.stream));
+    }
+  }
+  if (any_host || c.blocking) EXB_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+// Device status word written by kernels with bounded waits.
+int *device_status_word() { return reinterpret_cast<int *>(zero_words(64) + 32); }
+
+void set_status(int s) { tl_status = s; }
+
+void report(int status, const char *fn, const char *msg) {
+  tl_status = status;
+  if (g_handler) g_handler(status, fn, msg);
+}
+
+}  // namespace exb
+
+using namespace exb;
+
+extern "C" {
+
+int exoblas_get_status(void) { return tl_status; }
+
+const char *exoblas_status_string(int s) {
+  switch (s) {
+    case EXOBLAS_SUCCESS: return "success";
+    case EXOBLAS_UNSUPPORTED_ORDER: return "Order must be CblasRowMajor";
+    case EXOBLAS_INVALID_VALUE: return "invalid argument";
+    case EXOBLAS_CUDA_ERROR: return "CUDA error";
+    case EXOBLAS_ALLOC_FAILED: return "device allocation failed";
+    case EXOBLAS_TIMEOUT: return "kernel wait timed out";
+    case EXOBLAS_NOT_SUPPORTED: return "not supported on this device";
+    default: return "unknown status";
+  }
+}
+
+void exoblas_set_error_handler(exoblas_error_handler h) { g_handler = h; }
+
+int exoblas_set_stream(void *stream) {
+  return guarded("exoblas_set_stream", [&] {
+    Context &c = ctx();
+    EXB_CUDA(cudaStreamSynchronize(c.stream));
+    if (stream) {
+      if (c.own_stream) EXB_CUDA(cudaStreamDestroy(c.stream));
+      c.stream = static_cast<cudaStream_t>(stream);
+      c.own_stream = false;
+    } else if (!c.own_stream) {
+      EXB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+      c.own_stream = true;
+    }
+  });
+}
+
+void *exoblas_get_stream(void) {
+  void *s = nullptr;
+  guarded("exoblas_get_stream", [&] { s = ctx().stream; });
+  return s;
+}
+
+int exoblas_set_blocking(int b) {
+  return guarded("exoblas_set_blocking", [&] { ctx().blocking = b != 0; });
+}
+
+int exoblas_synchronize(void) {
+  return guarded("exoblas_synchronize", [&] { EXB_CUDA(cudaStreamSynchronize(ctx().stream)); });
+}
+
+int exoblas_set_precision(int mode) {
+  return guarded("exoblas_set_precision", [&] {
+    if (mode < EXOBLAS_PRECISION_NATIVE || mode > EXOBLAS_PRECISION_OZAKI)
+      fail(EXOBLAS_INVALID_VALUE, "unknown precision mode");
+    ctx().precision = mode;
+  });
+}
+
+int exoblas_get_precision(void) {
+  int p = EXOBLAS_PRECISION_NATIVE;
+  guarded("exoblas_get_precision", [&] { p = ctx().precision; });
+  return p;
+}
+
+unsigned long long exoblas_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+/*
+ * exoblas.h - C ABI of libexoblas_gb300.so, a GB300 (sm_103a) implementation
+ * of the ExoBLAS dense BLAS hot path.
+ *
+ * Every exo_<p><op> entry point keeps the signature, the CBLAS argument
+ * order, the flag values and the special cases of the ExoBLAS wrapper it
+ * replaces (cited beside each declaration as reference file:line).  Those
+ * wrappers are the C++ headers test/level{1,2,3}/<op>/exo_<op>_wrapper.h of
+ * exo-lang/ExoBLAS; they dispatch to Exo-generated CPU procs.  Here the same
+ * calls run hand-written CUDA kernels on the current CUDA device.
+ *
+ * Pointers may be host memory (pageable or pinned) or device memory
+ * (cudaMalloc / managed); the library asks the CUDA driver which one each
+ * pointer is.  Host operands are staged through device memory and copied
+ * back; device operands are used in place.  By default every call returns
+ * only after its results are visible to the caller (CBLAS semantics); see
+ * exoblas_set_blocking for the asynchronous device-pointer mode.
+ *
+ * Errors: the reference wrappers throw a C++ exception when Order is not
+ * CblasRowMajor (e.g. test/level3/gemm/exo_gemm_wrapper.h:15-17).  This
+ * library never throws across the ABI: it leaves every output untouched,
+ * records a status for the calling thread (exoblas_get_status) and, if one
+ * is installed, calls the error handler (exoblas_set_error_handler).
+ */
+#ifndef EXOBLAS_GB300_H
+#define EXOBLAS_GB300_H
+
+#if defined(__GNUC__)
+#define EXOBLAS_API __attribute__((visibility("default")))
+#else
+#define EXOBLAS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* CBLAS flag values, identical to test/common/cblas.h:10-18 of the reference
+ * (and to every netlib-compatible cblas.h, whose definitions are used when
+ * that header was included first). */
+#ifndef CBLAS_H
+enum CBLAS_ORDER { CblasRowMajor = 101, CblasColMajor = 102 };
+enum CBLAS_TRANSPOSE { CblasNoTrans = 111, CblasTrans = 112, CblasConjTrans = 113 };
+enum CBLAS_UPLO { CblasUpper = 121, CblasLower = 122 };
+enum CBLAS_DIAG { CblasNonUnit = 131, CblasUnit = 132 };
+enum CBLAS_SIDE { CblasLeft = 141, CblasRight = 142 };
+#endif
+
+/* ------------------------------------------------------------ status --- */
+enum EXOBLAS_STATUS {
+  EXOBLAS_SUCCESS = 0,
+  EXOBLAS_UNSUPPORTED_ORDER = 1, /* Order != CblasRowMajor (the reference throws) */
+  EXOBLAS_INVALID_VALUE = 2,     /* bad flag, negative size, lda too small, zero output stride */
+  EXOBLAS_CUDA_ERROR = 3,        /* a CUDA runtime call failed */
+  EXOBLAS_ALLOC_FAILED = 4,      /* device workspace or staging allocation failed */
+  EXOBLAS_TIMEOUT = 5,           /* a kernel's bounded wait ran out; outputs are undefined */
+  EXOBLAS_NOT_SUPPORTED = 6      /* requested mode not available on this device */
+};
+
+/* Status of the last exo_* / exoblas_* call made by the calling thread. */
+EXOBLAS_API int exoblas_get_status(void);
+EXOBLAS_API const char *exoblas_status_string(int status);
+/* Called (on the calling thread) whenever a call fails; NULL removes it. */
+typedef void (*exoblas_error_handler)(int status, const char *function, const char *message);
+EXOBLAS_API void exoblas_set_error_handler(exoblas_error_handler handler);
+
+/* ------------------------------------------------------ execution state - */
+/* Stream used by the calling thread's subsequent calls on the current device
+ * (a cudaStream_t; NULL selects the library's own non-blocking stream).
+ * Work already queued by this thread on its previous stream is synchronised
+ * first, so scratch memory is never shared by two streams at once. */
+EXOBLAS_API int exoblas_set_stream(void *stream);
+EXOBLAS_API void *exoblas_get_stream(void);
+/* blocking = 1 (default): calls return once results are visible on the host.
+ * blocking = 0: calls whose operands are ALL device pointers return after
+ * queuing their kernels on the thread's stream; scalar-returning reductions
+ * (asum, dot, dsdot, sdsdot) still wait for their result.  Use the
+ * exoblas_*_device variants below for fully asynchronous reductions. */
+EXOBLAS_API int exoblas_set_blocking(int blocking);
+EXOBLAS_API int exoblas_synchronize(void);
+
+/* Arithmetic used by exo_sgemm/ssymm/ssyrk and exo_dgemm:
+ *   EXOBLAS_PRECISION_NATIVE    FP32 FFMA / FP64 DFMA kernels (default)
+ *   EXOBLAS_PRECISION_SPLIT_BF16 sgemm/ssymm/ssyrk: each FP32 operand split
+ *                               into three BF16 terms, products on tcgen05
+ *                               tensor cores, FP32 accumulation
+ *   EXOBLAS_PRECISION_OZAKI     dgemm: Ozaki slice emulation with exact
+ *                               integer accumulation of small-integer slices
+ * The environment variable EXOBLAS_PRECISION_MODE (native | split_bf16 |
+ * ozaki) sets the initial value for every thread. */
+enum EXOBLAS_PRECISION { EXOBLAS_PRECISION_NATIVE = 0, EXOBLAS_PRECISION_SPLIT_BF16 = 1, EXOBLAS_PRECISION_OZAKI = 2 };
+EXOBLAS_API int exoblas_set_precision(int mode);
+EXOBLAS_API int exoblas_get_precision(void);
+
+/* Number of CUDA kernels this library has launched in the calling process. */
+EXOBLAS_API unsigned long long exoblas_kernel_launches(void);
+
+/* ------------------------------------------------------------ level 1 --- */
+/* test/level1/asum/exo_asum_wrapper.h:5-23 (incX < 0 returns 0) */
+EXOBLAS_API float exo_sasum(const int N, const float *X, const int incX);
+EXOBLAS_API double exo_dasum(const int N, const double *X, const int incX);
+/* test/level1/axpy/exo_axpy_wrapper.h:5-34 (alpha == 0 returns) */
+EXOBLAS_API void exo_saxpy(const int N, const float alpha, const float *X, const int incX, float *Y, const int incY);
+EXOBLAS_API void exo_daxpy(const int N, const double alpha, const double *X, const int incX, double *Y, const int incY);
+/* test/level1/dot/exo_dot_wrapper.h:5-27 */
+EXOBLAS_API float exo_sdot(const int N, const float *X, const int incX, const float *Y, const int incY);
+EXOBLAS_API double exo_ddot(const int N, const double *X, const int incX, const double *Y, const int incY);
+/* test/level1/dsdot/exo_dsdot_wrapper.h:5-25 */
+EXOBLAS_API double exo_dsdot(const int N, const float *X, const int incX, const float *Y, const int incY);
+/* test/level1/sdsdot/exo_sdsdot.h:5-26 */
+EXOBLAS_API float exo_sdsdot(const int N, const float alpha, const float *X, const int incX, const float *Y, const int incY);
+/* test/level1/copy/exo_copy_wrapper.h:5-23 */
+EXOBLAS_API void exo_scopy(const int N, const float *X, const int incX, float *Y, const int incY);
+EXOBLAS_API void exo_dcopy(const int N, const double *X, const int incX, double *Y, const int incY);
+/* test/level1/swap/exo_swap_wrapper.h:5-23 */
+EXOBLAS_API void exo_sswap(const int N, float *X, const int incX, float *Y, const int incY);
+EXOBLAS_API void exo_dswap(const int N, double *X, const int incX, double *Y, const int incY);
+/* test/level1/scal/exo_scal_wrapper.h:7-35 (alpha == 1 and incX < 0 return) */
+EXOBLAS_API void exo_sscal(const int N, const float alpha, float *X, const int incX);
+EXOBLAS_API void exo_dscal(const int N, const double alpha, double *X, const int incX);
+/* test/level1/rot/exo_rot_wrapper.h:5-23 */
+EXOBLAS_API void exo_srot(const int N, float *X, const int incX, float *Y, const int incY, const float c, const float s);
+EXOBLAS_API void exo_drot(const int N, double *X, const int incX, double *Y, const int incY, const double c, const double s);
+/* test/level1/rotm/exo_rotm_wrapper.h:5-44 (P[0] not in {-1, 0, 1}: no-op) */
+EXOBLAS_API void exo_srotm(const int N, float *X, const int incX, float *Y, const int incY, const float *P);
+EXOBLAS_API void exo_drotm(const int N, double *X, const int incX, double *Y, const int incY, const double *P);
+
+/* Device-result reductions (no counterpart in the reference: the reference
+ * returns the scalar).  All pointers must be device pointers; *result is
+ * written by a kernel on the thread's stream and the call does not wait. */
+EXOBLAS_API int exoblas_sasum_device(const int N, const float *X, const int incX, float *result);
+EXOBLAS_API int exoblas_dasum_device(const int N, const double *X, const int incX, double *result);
+EXOBLAS_API int exoblas_sdot_device(const int N, const float *X, const int incX, const float *Y, const int incY, float *result);
+EXOBLAS_API int exoblas_ddot_device(const int N, const double *X, const int incX, const double *Y, const int incY, double *result);
+EXOBLAS_API int exoblas_dsdot_device(const int N, const float *X, const int incX, const float *Y, const int incY, double *result);
+
+/* ------------------------------------------------------------ level 2 --- */
+/* test/level2/gemv/exo_gemv_wrapper.h:7-39 */
+EXOBLAS_API void exo_sgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N, const float alpha,
+               const float *A, const int lda, const float *X, const int incX, const float beta, float *Y, const int incY);
+EXOBLAS_API void exo_dgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N, const double alpha,
+               const double *A, const int lda, const double *X, const int incX, const double beta, double *Y, const int incY);
+/* test/level2/ger/exo_ger_wrapper.h:7-34 (Order is not checked; alpha == 0 returns) */
+EXOBLAS_API void exo_sger(const enum CBLAS_ORDER order, const int M, const int N, const float alpha, const float *X, const int incX,
+              const float *Y, const int incY, float *A, const int lda);
+EXOBLAS_API void exo_dger(const enum CBLAS_ORDER order, const int M, const int N, const double alpha, const double *X, const int incX,
+              const double *Y, const int incY, double *A, const int lda);
+/* test/level2/symv/exo_symv_wrapper.h:7-34 */
+EXOBLAS_API void exo_ssymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha, const float *A,
+               const int lda, const float *X, const int incX, const float beta, float *Y, const int incY);
+EXOBLAS_API void exo_dsymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha, const double *A,
+               const int lda, const double *X, const int incX, const double beta, double *Y, const int incY);
+/* test/level2/syr/exo_syr_wrapper.h:5-32 (alpha == 0 returns) */
+EXOBLAS_API void exo_ssyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha, const float *X,
+              const int incX, float *A, const int lda);
+EXOBLAS_API void exo_dsyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha, const double *X,
+              const int incX, double *A, const int lda);
+/* test/level2/syr2/exo_syr2_wrapper.h:5-36 (Order is not checked; alpha == 0 returns) */
+EXOBLAS_API void exo_ssyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha, const float *X,
+               const int incX, const float *Y, const int incY, float *A, const int lda);
+EXOBLAS_API void exo_dsyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha, const double *X,
+               const int incX, const double *Y, const int incY, double *A, const int lda);
+/* test/level2/trmv/exo_trmv_wrapper.h:7-29 */
+EXOBLAS_API void exo_strmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX);
+EXOBLAS_API void exo_dtrmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX);
+/* test/level2/trsv/exo_trsv_wrapper.h:7-29 */
+EXOBLAS_API void exo_strsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX);
+EXOBLAS_API void exo_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX);
+
+/* ------------------------------------------------------------ level 3 --- */
+/* test/level3/gemm/exo_gemm_wrapper.h:9-28 (C *= beta, then C += alpha op(A) op(B)) */
+EXOBLAS_API void exo_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
+               const int M, const int N, const int K, const float alpha, const float *A, const int lda, const float *B,
+               const int ldb, const float beta, float *C, const int ldc);
+EXOBLAS_API void exo_dgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
+               const int M, const int N, const int K, const double alpha, const double *A, const int lda,
+               const double *B, const int ldb, const double beta, double *C, const int ldc);
+/* test/level3/symm/exo_symm_wrapper.h:9-27 */
+EXOBLAS_API void exo_ssymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
+               const int N, const float alpha, const float *A, const int lda, const float *B, const int ldb,
+               const float beta, float *C, const int ldc);
+EXOBLAS_API void exo_dsymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
+               const int N, const double alpha, const double *A, const int lda, const double *B, const int ldb,
+               const double beta, double *C, const int ldc);
+/* test/level3/syrk/exo_syrk_wrapper.h:9-28 (the triangle of C *= beta, then the update) */
+EXOBLAS_API void exo_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans, const int N,
+               const int K, const float alpha, const float *A, const int lda, const float beta, float *C,
+               const int ldc);
+EXOBLAS_API void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans, const int N,
+               const int K, const double alpha, const double *A, const int lda, const double beta, double *C,
+               const int ldc);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXOBLAS_GB300_H */

@@ -1,0 +1,873 @@
+// CPU oracle for the exoblas_gb300 BLAS hot path. TEST INFRASTRUCTURE ONLY.
+//
+// This file restates, in plain C++, the algorithm of every in-scope ExoBLAS
+// `@proc` (the unscheduled loop nest, in its loop order) together with the
+// CBLAS-order wrapper that dispatches to it (flag checks, negative-increment
+// rebasing, alpha/beta special cases, beta pre-scaling for level 3).  It is
+// the checker for the GPU library and the CPU baseline timed beside it; it is
+// never linked into, loaded by or called from the GPU library itself.
+//
+// Each function cites the reference file:line it follows.  Sources:
+//   src/level1/{asum,axpy,dot,dsdot,exo_copy,rot,rotm,scal,swap}.py
+//   src/level2/{gemv,ger,symv,syr,syr2,trmv,trsv}.py
+//   src/level3/{gemm,symm,syrk,mscal}.py
+//   test/level*/<op>/exo_<op>_wrapper.h, test/level1/sdsdot/exo_sdsdot.h
+//
+// The reference raises a C++ exception when Order != RowMajor.  The oracle
+// records status 1 (read with oracle_last_status()) and returns instead.
+//
+// Also here: double-double reference kernels (TwoSum after Knuth, TwoProd via
+// fma after Dekker 1971, Dot2 after Ogita, Rump and Oishi 2005) used as the
+// high-precision oracle for d-precision results, and multi-threaded drivers
+// of the same algorithms (row / range partitions over std::thread) used only
+// to time the CPU baseline on all host cores.
+
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// CBLAS flag values (src/common/cblas_enums.py:4-33, test/common/cblas.h:10-18)
+constexpr int kRowMajor = 101;
+constexpr int kNoTrans = 111;
+constexpr int kUpper = 121;
+constexpr int kLower = 122;
+constexpr int kNonUnit = 131;
+constexpr int kUnit = 132;
+constexpr int kLeft = 141;
+
+thread_local int g_status = 0;
+
+inline bool row_major_or_fail(int order) {
+  if (order != kRowMajor) {
+    g_status = 1;
+    return false;
+  }
+  return true;
+}
+
+// A strided 1-D window: element i lives at p[i * s] (s may be negative after
+// the wrapper rebased the pointer, exactly as the reference wrappers do).
+template <typename T>
+struct Vec {
+  T *p;
+  long s;
+  T &operator[](long i) const { return p[i * s]; }
+};
+
+// A row-major 2-D window with leading dimension ld and unit inner stride.
+template <typename T>
+struct Mat {
+  T *p;
+  long ld;
+  T &operator()(long i, long j) const { return p[i * ld + j]; }
+};
+
+template <typename T>
+T *rebase(T *x, int n, int inc) {
+  // exo_axpy_wrapper.h:23-28 and every other wrapper: X + (1 - N) * incX
+  return inc < 0 ? x + (long)(1 - n) * inc : x;
+}
+
+// ---------------------------------------------------------------- level 1 --
+
+// src/level1/asum.py:11-15 (select(0, x, x, -x) == |x|)
+template <typename T>
+T asum_proc(long n, Vec<T> x) {
+  T result = 0.0;
+  for (long i = 0; i < n; ++i) result += (T(0) < x[i]) ? x[i] : -x[i];
+  return result;
+}
+
+// test/level1/asum/exo_asum_wrapper.h:5-23 (incX < 0 returns 0)
+template <typename T>
+T asum_wrap(int N, const T *X, int incX) {
+  g_status = 0;
+  if (incX != 1 && incX < 0) return 0.0;
+  return asum_proc<T>(N, Vec<T>{const_cast<T *>(X), incX});
+}
+
+// src/level1/axpy.py:9-19
+template <typename T>
+void axpy_proc(long n, T alpha, Vec<T> x, Vec<T> y) {
+  for (long i = 0; i < n; ++i) y[i] += alpha * x[i];
+}
+template <typename T>
+void axpy_alpha_1_proc(long n, Vec<T> x, Vec<T> y) {
+  for (long i = 0; i < n; ++i) y[i] += x[i];
+}
+
+// test/level1/axpy/exo_axpy_wrapper.h:5-34
+template <typename T>
+void axpy_wrap(int N, T alpha, const T *X, int incX, T *Y, int incY) {
+  g_status = 0;
+  if (alpha == 0.0) return;
+  if (incX == 1 && incY == 1) {
+    if (alpha == 1.0)
+      axpy_alpha_1_proc<T>(N, Vec<T>{const_cast<T *>(X), 1}, Vec<T>{Y, 1});
+    else
+      axpy_proc<T>(N, alpha, Vec<T>{const_cast<T *>(X), 1}, Vec<T>{Y, 1});
+  } else {
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+    axpy_proc<T>(N, alpha, Vec<T>{const_cast<T *>(X), incX}, Vec<T>{Y, incY});
+  }
+}
+
+// src/level1/dot.py:9-13
+template <typename T>
+T dot_proc(long n, Vec<T> x, Vec<T> y) {
+  T result = 0.0;
+  for (long i = 0; i < n; ++i) result += x[i] * y[i];
+  return result;
+}
+
+// test/level1/dot/exo_dot_wrapper.h:5-27
+template <typename T>
+T dot_wrap(int N, const T *X, int incX, const T *Y, int incY) {
+  g_status = 0;
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+  }
+  return dot_proc<T>(N, Vec<T>{const_cast<T *>(X), incX},
+                     Vec<T>{const_cast<T *>(Y), incY});
+}
+
+// src/level1/dsdot.py:11-21
+double dsdot_proc(long n, Vec<float> x, Vec<float> y) {
+  double d_dot = 0.0;
+  for (long i = 0; i < n; ++i) {
+    double d_x = x[i];
+    double d_y = y[i];
+    d_dot += d_x * d_y;
+  }
+  return d_dot;
+}
+
+// src/level1/dsdot.py:24-36
+float sdsdot_proc(long n, float sb, Vec<float> x, Vec<float> y) {
+  double d_dot = dsdot_proc(n, x, y);
+  double d_result = d_dot;
+  d_result += sb;
+  return (float)d_result;
+}
+
+// src/level1/exo_copy.py:9-12
+template <typename T>
+void copy_proc(long n, Vec<T> x, Vec<T> y) {
+  for (long i = 0; i < n; ++i) y[i] = x[i];
+}
+
+// src/level1/swap.py:9-15
+template <typename T>
+void swap_proc(long n, Vec<T> x, Vec<T> y) {
+  for (long i = 0; i < n; ++i) {
+    T tmp = x[i];
+    x[i] = y[i];
+    y[i] = tmp;
+  }
+}
+
+// src/level1/scal.py:9-19
+template <typename T>
+void scal_proc(long n, T alpha, Vec<T> x) {
+  for (long i = 0; i < n; ++i) x[i] = alpha * x[i];
+}
+template <typename T>
+void scal_alpha_0_proc(long n, Vec<T> x) {
+  for (long i = 0; i < n; ++i) x[i] = 0.0;
+}
+
+// test/level1/scal/exo_scal_wrapper.h:7-35
+template <typename T>
+void scal_wrap(int N, T alpha, T *X, int incX) {
+  g_status = 0;
+  if (alpha == 1.0) return;
+  if (incX != 1 && incX < 0) return;
+  if (alpha == 0.0)
+    scal_alpha_0_proc<T>(N, Vec<T>{X, incX});
+  else
+    scal_proc<T>(N, alpha, Vec<T>{X, incX});
+}
+
+// src/level1/rot.py:9-15
+template <typename T>
+void rot_proc(long n, Vec<T> x, Vec<T> y, T c, T s) {
+  for (long i = 0; i < n; ++i) {
+    T xReg = x[i];
+    x[i] = c * xReg + s * y[i];
+    y[i] = -s * xReg + c * y[i];
+  }
+}
+
+// src/level1/rotm.py:9-33 with H = {P[1], P[3], P[2], P[4]} as a row-major
+// 2x2 (test/level1/rotm/exo_rotm_wrapper.h:8); flags other than -1, 0, 1
+// (e.g. -2) leave x and y untouched (exo_rotm_wrapper.h:10-22).
+template <typename T>
+void rotm_proc(long n, Vec<T> x, Vec<T> y, const T *P) {
+  const T h00 = P[1], h01 = P[3], h10 = P[2], h11 = P[4];
+  const T flag = P[0];
+  for (long i = 0; i < n; ++i) {
+    T xReg = x[i];
+    if (flag == -1.0) {
+      x[i] = h00 * xReg + h01 * y[i];
+      y[i] = h10 * xReg + h11 * y[i];
+    } else if (flag == 0.0) {
+      x[i] = xReg + h01 * y[i];
+      y[i] = h10 * xReg + y[i];
+    } else if (flag == 1.0) {
+      x[i] = h00 * xReg + y[i];
+      y[i] = -xReg + h11 * y[i];
+    } else {
+      return;
+    }
+  }
+}
+
+template <typename T>
+void two_vec_wrap_prep(int N, T *&X, int incX, T *&Y, int incY) {
+  g_status = 0;
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+  }
+}
+
+// ---------------------------------------------------------------- level 2 --
+
+// src/level2/gemv.py:10-22; wrapper test/level2/gemv/exo_gemv_wrapper.h:7-39
+template <typename T>
+void gemv_wrap(int order, int TransA, int M, int N, T alpha, const T *A,
+               int lda, const T *X, int incX, T beta, T *Y, int incY) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  const int m = TransA == kNoTrans ? M : N;  // length of y
+  const int n = TransA == kNoTrans ? N : M;  // length of x
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, n, incX);
+    Y = rebase(Y, m, incY);
+  }
+  Vec<T> x{const_cast<T *>(X), incX}, y{Y, incY};
+  Mat<T> a{const_cast<T *>(A), lda};
+  for (long i = 0; i < m; ++i) y[i] = y[i] * beta;
+  if (TransA == kNoTrans) {
+    for (long i = 0; i < m; ++i)
+      for (long j = 0; j < n; ++j) y[i] += alpha * (x[j] * a(i, j));
+  } else {
+    // AT has shape [n, m] (the caller's M x N matrix)
+    for (long i = 0; i < n; ++i)
+      for (long j = 0; j < m; ++j) y[j] += alpha * x[i] * a(i, j);
+  }
+}
+
+// src/level2/ger.py:9-15; wrapper test/level2/ger/exo_ger_wrapper.h:7-34
+// (the wrapper does not check Order)
+template <typename T>
+void ger_wrap(int order, int M, int N, T alpha, const T *X, int incX,
+              const T *Y, int incY, T *A, int lda) {
+  (void)order;
+  g_status = 0;
+  if (alpha == 0.0) return;
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, M, incX);
+    Y = rebase(Y, N, incY);
+  }
+  Vec<T> x{const_cast<T *>(X), incX}, y{const_cast<T *>(Y), incY};
+  Mat<T> a{A, lda};
+  for (long i = 0; i < M; ++i)
+    for (long j = 0; j < N; ++j) a(i, j) += alpha * x[i] * y[j];
+}
+
+// src/level2/symv.py:10-35; wrapper test/level2/symv/exo_symv_wrapper.h:7-34
+template <typename T>
+void symv_wrap(int order, int Uplo, int N, T alpha, const T *A, int lda,
+               const T *X, int incX, T beta, T *Y, int incY) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  X = rebase(X, N, incX);
+  Y = rebase(Y, N, incY);
+  Vec<T> x{const_cast<T *>(X), incX}, y{Y, incY};
+  Mat<T> a{const_cast<T *>(A), lda};
+  const long n = N;
+  for (long i = 0; i < n; ++i) y[i] = beta * y[i];
+  for (long i = 0; i < n; ++i) {
+    if (Uplo == kUpper) {
+      const long ii = n - i - 1;
+      T temp = alpha * x[ii];
+      T dot = 0.0;
+      for (long j = 0; j < i + 1; ++j) {
+        const long jj = n - j - 1;
+        y[jj] += temp * a(ii, jj);
+        dot += a(ii, jj) * x[jj];
+      }
+      y[ii] += alpha * (dot - a(ii, ii) * x[ii]);
+    } else {
+      T temp = alpha * x[i];
+      T dot = 0.0;
+      for (long j = 0; j < i + 1; ++j) {
+        y[j] += temp * a(i, j);
+        dot += a(i, j) * x[j];
+      }
+      y[i] += alpha * (dot - a(i, i) * x[i]);
+    }
+  }
+}
+
+// src/level2/syr.py:10-19; wrapper test/level2/syr/exo_syr_wrapper.h:5-32
+template <typename T>
+void syr_wrap(int order, int Uplo, int N, T alpha, const T *X, int incX, T *A,
+              int lda) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  if (alpha == 0.0) return;
+  if (incX != 1) X = rebase(X, N, incX);
+  Vec<T> x{const_cast<T *>(X), incX};
+  Mat<T> a{A, lda};
+  const long n = N;
+  for (long i = 0; i < n; ++i)
+    for (long j = 0; j < i + 1; ++j) {
+      if (Uplo == kUpper)
+        a(n - i - 1, n - j - 1) += (alpha * x[n - i - 1]) * x[n - j - 1];
+      else
+        a(i, j) += alpha * x[i] * x[j];
+    }
+}
+
+// src/level2/syr2.py:9-27; wrapper test/level2/syr2/exo_syr2_wrapper.h:5-36
+// (the wrapper does not check Order)
+template <typename T>
+void syr2_wrap(int order, int Uplo, int N, T alpha, const T *X, int incX,
+               const T *Y, int incY, T *A, int lda) {
+  (void)order;
+  g_status = 0;
+  if (alpha == 0.0) return;
+  X = rebase(X, N, incX);
+  Y = rebase(Y, N, incY);
+  Vec<T> x{const_cast<T *>(X), incX}, y{const_cast<T *>(Y), incY};
+  Mat<T> a{A, lda};
+  const long n = N;
+  for (long i = 0; i < n; ++i)
+    for (long j = 0; j < i + 1; ++j) {
+      if (Uplo == kUpper) {
+        const long ii = n - i - 1, jj = n - j - 1;
+        a(ii, jj) += (alpha * x[ii]) * y[jj] + (alpha * y[ii]) * x[jj];
+      } else {
+        a(i, j) += (alpha * x[i]) * y[j] + (alpha * y[i]) * x[j];
+      }
+    }
+}
+
+// src/level2/trmv.py:9-43; wrapper test/level2/trmv/exo_trmv_wrapper.h:7-29
+template <typename T>
+void trmv_wrap(int order, int Uplo, int TransA, int Diag, int N, const T *A,
+               int lda, T *X, int incX) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  X = rebase(X, N, incX);
+  Vec<T> x{X, incX};
+  Mat<T> a{const_cast<T *>(A), lda};
+  const long n = N;
+  std::vector<T> xCopy(n > 0 ? n : 0, T(0));
+  for (long i = 0; i < n; ++i) {
+    if (TransA == kNoTrans) {
+      if (Uplo == kUpper) {
+        const long ii = n - i - 1;
+        for (long j = 0; j < i + 1; ++j)
+          xCopy[ii] += a(ii, n - j - 1) * x[n - j - 1];
+        if (Diag == kUnit) xCopy[ii] += (1 - a(ii, ii)) * x[ii];
+      } else {
+        for (long j = 0; j < i + 1; ++j) xCopy[i] += a(i, j) * x[j];
+        if (Diag == kUnit) xCopy[i] += (1 - a(i, i)) * x[i];
+      }
+    } else {
+      if (Uplo == kUpper) {
+        const long ii = n - i - 1;
+        for (long j = 0; j < i + 1; ++j)
+          xCopy[n - j - 1] += a(ii, n - j - 1) * x[ii];
+        if (Diag == kUnit) xCopy[ii] += (1 - a(ii, ii)) * x[ii];
+      } else {
+        for (long j = 0; j < i + 1; ++j) xCopy[j] += a(i, j) * x[i];
+        if (Diag == kUnit) xCopy[i] += (1 - a(i, i)) * x[i];
+      }
+    }
+  }
+  for (long l = 0; l < n; ++l) x[l] = xCopy[l];
+}
+
+// src/level2/trsv.py:10-52; wrapper test/level2/trsv/exo_trsv_wrapper.h:7-29
+template <typename T>
+void trsv_wrap(int order, int Uplo, int TransA, int Diag, int N, const T *A,
+               int lda, T *X, int incX) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  X = rebase(X, N, incX);
+  Vec<T> x{X, incX};
+  Mat<T> a{const_cast<T *>(A), lda};
+  const long n = N;
+  std::vector<T> Dot(n > 0 ? n : 0, T(0));
+  for (long i = 0; i < n; ++i) {
+    if (TransA == kNoTrans) {
+      T dot = 0.0;
+      if (Uplo == kUpper) {
+        const long ii = n - i - 1;
+        for (long j = 0; j < i; ++j) dot += a(ii, n - j - 1) * x[n - j - 1];
+        x[ii] = x[ii] - dot;
+        if (Diag == kNonUnit) x[ii] = x[ii] / a(ii, ii);
+      } else {
+        for (long j = 0; j < i; ++j) dot += a(i, j) * x[j];
+        x[i] = x[i] - dot;
+        if (Diag == kNonUnit) x[i] = x[i] / a(i, i);
+      }
+    } else {
+      if (Uplo == kUpper) {
+        x[i] = x[i] - Dot[i];
+        if (Diag == kNonUnit) x[i] = x[i] / a(i, i);
+        for (long j = 0; j < n - i - 1; ++j)
+          Dot[n - j - 1] += a(i, n - j - 1) * x[i];
+      } else {
+        const long ii = n - i - 1;
+        x[ii] = x[ii] - Dot[ii];
+        if (Diag == kNonUnit) x[ii] = x[ii] / a(ii, ii);
+        for (long j = 0; j < n - i - 1; ++j) Dot[j] += a(ii, j) * x[ii];
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- level 3 --
+
+// src/level3/mscal.py:12-18 (full matrix) and :21-28 (one triangle)
+template <typename T>
+void mscal_proc(long M, long N, T beta, Mat<T> c) {
+  for (long i = 0; i < M; ++i)
+    for (long j = 0; j < N; ++j) c(i, j) = c(i, j) * beta;
+}
+template <typename T>
+void trmscal_proc(int Uplo, long N, T beta, Mat<T> c) {
+  for (long i = 0; i < N; ++i)
+    for (long j = 0; j < N; ++j)
+      if ((Uplo == kUpper && j >= i) || (Uplo == kLower && j < i + 1))
+        c(i, j) = c(i, j) * beta;
+}
+
+// src/level3/gemm.py:17-47 over the row range [i0, i1).  Per element of C the
+// k-sum runs in increasing k exactly as in the i,j,k nest; the i,k,j order
+// used here only changes which element is touched next, not the sum order.
+template <typename T>
+void gemm_rows(int TransA, int TransB, long i0, long i1, long N, long K,
+               T alpha, Mat<T> a, Mat<T> b, Mat<T> c) {
+  for (long i = i0; i < i1; ++i) {
+    T *ci = &c(i, 0);
+    if (TransB == kNoTrans) {
+      for (long k = 0; k < K; ++k) {
+        const T aik = TransA == kNoTrans ? a(i, k) : a(k, i);
+        const T *bk = &b(k, 0);
+        for (long j = 0; j < N; ++j) ci[j] += alpha * (aik * bk[j]);
+      }
+    } else {
+      for (long j = 0; j < N; ++j) {
+        T acc = ci[j];
+        const T *bj = &b(j, 0);
+        for (long k = 0; k < K; ++k) {
+          const T aik = TransA == kNoTrans ? a(i, k) : a(k, i);
+          acc += alpha * (aik * bj[k]);
+        }
+        ci[j] = acc;
+      }
+    }
+  }
+}
+
+// test/level3/gemm/exo_gemm_wrapper.h:9-28: C *= beta (mscal), then the proc
+template <typename T>
+void gemm_wrap(int order, int TransA, int TransB, int M, int N, int K,
+               T alpha, const T *A, int lda, const T *B, int ldb, T beta, T *C,
+               int ldc) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  Mat<T> a{const_cast<T *>(A), lda}, b{const_cast<T *>(B), ldb}, c{C, ldc};
+  mscal_proc<T>(M, N, beta, c);
+  gemm_rows<T>(TransA, TransB, 0, M, N, K, alpha, a, b, c);
+}
+
+// src/level3/symm.py:16-47 over the row range [i0, i1)
+template <typename T>
+void symm_rows(int Side, int Uplo, long i0, long i1, long M, long N, T alpha,
+               Mat<T> a, Mat<T> b, Mat<T> c) {
+  for (long i = i0; i < i1; ++i) {
+    T *ci = &c(i, 0);
+    if (Side == kLeft) {
+      for (long k = 0; k < M; ++k) {
+        T a_val;
+        if (Uplo == kUpper)
+          a_val = k < i + 1 ? a(k, i) : a(i, k);
+        else
+          a_val = k < i + 1 ? a(i, k) : a(k, i);
+        const T *bk = &b(k, 0);
+        for (long j = 0; j < N; ++j) ci[j] += alpha * (a_val * bk[j]);
+      }
+    } else {
+      for (long k = 0; k < N; ++k) {
+        const T bik = b(i, k);
+        for (long j = 0; j < N; ++j) {
+          T a_val;
+          if (Uplo == kUpper)
+            a_val = j < k + 1 ? a(j, k) : a(k, j);
+          else
+            a_val = j < k + 1 ? a(k, j) : a(j, k);
+          ci[j] += alpha * (bik * a_val);
+        }
+      }
+    }
+  }
+}
+
+// test/level3/symm/exo_symm_wrapper.h:9-27
+template <typename T>
+void symm_wrap(int order, int Side, int Uplo, int M, int N, T alpha,
+               const T *A, int lda, const T *B, int ldb, T beta, T *C,
+               int ldc) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  Mat<T> a{const_cast<T *>(A), lda}, b{const_cast<T *>(B), ldb}, c{C, ldc};
+  mscal_proc<T>(M, N, beta, c);
+  symm_rows<T>(Side, Uplo, 0, M, M, N, alpha, a, b, c);
+}
+
+// src/level3/syrk.py:17-32 over the row range [i0, i1)
+template <typename T>
+void syrk_rows(int Uplo, int Trans, long i0, long i1, long N, long K, T alpha,
+               Mat<T> a, Mat<T> c) {
+  for (long i = i0; i < i1; ++i) {
+    const long j0 = Uplo == kUpper ? i : 0;
+    const long j1 = Uplo == kUpper ? N : i + 1;
+    T *ci = &c(i, 0);
+    if (Trans == kNoTrans) {
+      const T *ai = &a(i, 0);
+      for (long j = j0; j < j1; ++j) {
+        const T *aj = &a(j, 0);
+        T acc = ci[j];
+        for (long k = 0; k < K; ++k) acc += alpha * (ai[k] * aj[k]);
+        ci[j] = acc;
+      }
+    } else {
+      for (long k = 0; k < K; ++k) {
+        const T aki = a(k, i);
+        const T *ak = &a(k, 0);
+        for (long j = j0; j < j1; ++j) ci[j] += alpha * (aki * ak[j]);
+      }
+    }
+  }
+}
+
+// test/level3/syrk/exo_syrk_wrapper.h:9-28: trmscal then the proc
+template <typename T>
+void syrk_wrap(int order, int Uplo, int Trans, int N, int K, T alpha,
+               const T *A, int lda, T beta, T *C, int ldc) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  Mat<T> a{const_cast<T *>(A), lda}, c{C, ldc};
+  trmscal_proc<T>(Uplo, N, beta, c);
+  syrk_rows<T>(Uplo, Trans, 0, N, N, K, alpha, a, c);
+}
+
+// --------------------------------------------------- double-double oracle --
+// TwoSum (Knuth, TAOCP vol. 2), TwoProd through fma (Dekker 1971),
+// Dot2 (Ogita, Rump, Oishi, "Accurate sum and dot product", SISC 2005).
+
+struct DD {
+  double hi, lo;
+};
+inline void two_sum(double a, double b, double &s, double &e) {
+  s = a + b;
+  double z = s - a;
+  e = (a - (s - z)) + (b - z);
+}
+inline void two_prod(double a, double b, double &p, double &e) {
+  p = a * b;
+  e = std::fma(a, b, -p);
+}
+inline void dd_add_prod(DD &acc, double a, double b) {
+  double p, pe, s, se;
+  two_prod(a, b, p, pe);
+  two_sum(acc.hi, p, s, se);
+  acc.hi = s;
+  acc.lo += pe + se;
+}
+inline DD dd_norm(DD v) {
+  double s, e;
+  two_sum(v.hi, v.lo, s, e);
+  return DD{s, e};
+}
+
+// ------------------------------------------------------ threaded drivers --
+
+template <typename F>
+void parallel_for(int nthreads, long n, F f) {
+  if (nthreads <= 1 || n < 2) {
+    f(0, 0, n);
+    return;
+  }
+  if (nthreads > n) nthreads = (int)n;
+  std::vector<std::thread> th;
+  th.reserve(nthreads);
+  for (int t = 0; t < nthreads; ++t) {
+    long lo = n * t / nthreads, hi = n * (t + 1) / nthreads;
+    th.emplace_back([=] { f(t, lo, hi); });
+  }
+  for (auto &x : th) x.join();
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ C interface --
+
+#define ORACLE_API extern "C" __attribute__((visibility("default")))
+
+ORACLE_API int oracle_last_status(void) { return g_status; }
+
+ORACLE_API float oracle_sasum(int N, const float *X, int incX) { return asum_wrap<float>(N, X, incX); }
+ORACLE_API double oracle_dasum(int N, const double *X, int incX) { return asum_wrap<double>(N, X, incX); }
+
+ORACLE_API void oracle_saxpy(int N, float alpha, const float *X, int incX, float *Y, int incY) { axpy_wrap<float>(N, alpha, X, incX, Y, incY); }
+ORACLE_API void oracle_daxpy(int N, double alpha, const double *X, int incX, double *Y, int incY) { axpy_wrap<double>(N, alpha, X, incX, Y, incY); }
+
+ORACLE_API float oracle_sdot(int N, const float *X, int incX, const float *Y, int incY) { return dot_wrap<float>(N, X, incX, Y, incY); }
+ORACLE_API double oracle_ddot(int N, const double *X, int incX, const double *Y, int incY) { return dot_wrap<double>(N, X, incX, Y, incY); }
+
+// test/level1/dsdot/exo_dsdot_wrapper.h:5-25
+ORACLE_API double oracle_dsdot(int N, const float *X, int incX, const float *Y, int incY) {
+  g_status = 0;
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+  }
+  return dsdot_proc(N, Vec<float>{const_cast<float *>(X), incX}, Vec<float>{const_cast<float *>(Y), incY});
+}
+// test/level1/sdsdot/exo_sdsdot.h:5-26
+ORACLE_API float oracle_sdsdot(int N, float alpha, const float *X, int incX, const float *Y, int incY) {
+  g_status = 0;
+  if (!(incX == 1 && incY == 1)) {
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+  }
+  return sdsdot_proc(N, alpha, Vec<float>{const_cast<float *>(X), incX}, Vec<float>{const_cast<float *>(Y), incY});
+}
+
+// test/level1/copy/exo_copy_wrapper.h:5-23
+ORACLE_API void oracle_scopy(int N, const float *X, int incX, float *Y, int incY) {
+  float *x = const_cast<float *>(X);
+  two_vec_wrap_prep<float>(N, x, incX, Y, incY);
+  copy_proc<float>(N, Vec<float>{x, incX}, Vec<float>{Y, incY});
+}
+ORACLE_API void oracle_dcopy(int N, const double *X, int incX, double *Y, int incY) {
+  double *x = const_cast<double *>(X);
+  two_vec_wrap_prep<double>(N, x, incX, Y, incY);
+  copy_proc<double>(N, Vec<double>{x, incX}, Vec<double>{Y, incY});
+}
+// test/level1/swap/exo_swap_wrapper.h:5-23
+ORACLE_API void oracle_sswap(int N, float *X, int incX, float *Y, int incY) {
+  two_vec_wrap_prep<float>(N, X, incX, Y, incY);
+  swap_proc<float>(N, Vec<float>{X, incX}, Vec<float>{Y, incY});
+}
+ORACLE_API void oracle_dswap(int N, double *X, int incX, double *Y, int incY) {
+  two_vec_wrap_prep<double>(N, X, incX, Y, incY);
+  swap_proc<double>(N, Vec<double>{X, incX}, Vec<double>{Y, incY});
+}
+ORACLE_API void oracle_sscal(int N, float alpha, float *X, int incX) { scal_wrap<float>(N, alpha, X, incX); }
+ORACLE_API void oracle_dscal(int N, double alpha, double *X, int incX) { scal_wrap<double>(N, alpha, X, incX); }
+// test/level1/rot/exo_rot_wrapper.h:5-23
+ORACLE_API void oracle_srot(int N, float *X, int incX, float *Y, int incY, float c, float s) {
+  two_vec_wrap_prep<float>(N, X, incX, Y, incY);
+  rot_proc<float>(N, Vec<float>{X, incX}, Vec<float>{Y, incY}, c, s);
+}
+ORACLE_API void oracle_drot(int N, double *X, int incX, double *Y, int incY, double c, double s) {
+  two_vec_wrap_prep<double>(N, X, incX, Y, incY);
+  rot_proc<double>(N, Vec<double>{X, incX}, Vec<double>{Y, incY}, c, s);
+}
+// test/level1/rotm/exo_rotm_wrapper.h:5-44
+ORACLE_API void oracle_srotm(int N, float *X, int incX, float *Y, int incY, const float *P) {
+  two_vec_wrap_prep<float>(N, X, incX, Y, incY);
+  rotm_proc<float>(N, Vec<float>{X, incX}, Vec<float>{Y, incY}, P);
+}
+ORACLE_API void oracle_drotm(int N, double *X, int incX, double *Y, int incY, const double *P) {
+  two_vec_wrap_prep<double>(N, X, incX, Y, incY);
+  rotm_proc<double>(N, Vec<double>{X, incX}, Vec<double>{Y, incY}, P);
+}
+
+ORACLE_API void oracle_sgemv(int order, int TransA, int M, int N, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { gemv_wrap<float>(order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dgemv(int order, int TransA, int M, int N, double alpha, const double *A, int lda, const double *X, int incX, double beta, double *Y, int incY) { gemv_wrap<double>(order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_sger(int order, int M, int N, float alpha, const float *X, int incX, const float *Y, int incY, float *A, int lda) { ger_wrap<float>(order, M, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_dger(int order, int M, int N, double alpha, const double *X, int incX, const double *Y, int incY, double *A, int lda) { ger_wrap<double>(order, M, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_ssymv(int order, int Uplo, int N, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { symv_wrap<float>(order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dsymv(int order, int Uplo, int N, double alpha, const double *A, int lda, const double *X, int incX, double beta, double *Y, int incY) { symv_wrap<double>(order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_ssyr(int order, int Uplo, int N, float alpha, const float *X, int incX, float *A, int lda) { syr_wrap<float>(order, Uplo, N, alpha, X, incX, A, lda); }
+ORACLE_API void oracle_dsyr(int order, int Uplo, int N, double alpha, const double *X, int incX, double *A, int lda) { syr_wrap<double>(order, Uplo, N, alpha, X, incX, A, lda); }
+ORACLE_API void oracle_ssyr2(int order, int Uplo, int N, float alpha, const float *X, int incX, const float *Y, int incY, float *A, int lda) { syr2_wrap<float>(order, Uplo, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_dsyr2(int order, int Uplo, int N, double alpha, const double *X, int incX, const double *Y, int incY, double *A, int lda) { syr2_wrap<double>(order, Uplo, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_strmv(int order, int Uplo, int TransA, int Diag, int N, const float *A, int lda, float *X, int incX) { trmv_wrap<float>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+ORACLE_API void oracle_dtrmv(int order, int Uplo, int TransA, int Diag, int N, const double *A, int lda, double *X, int incX) { trmv_wrap<double>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+ORACLE_API void oracle_strsv(int order, int Uplo, int TransA, int Diag, int N, const float *A, int lda, float *X, int incX) { trsv_wrap<float>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+ORACLE_API void oracle_dtrsv(int order, int Uplo, int TransA, int Diag, int N, const double *A, int lda, double *X, int incX) { trsv_wrap<double>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+
+ORACLE_API void oracle_sgemm(int order, int TransA, int TransB, int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc) { gemm_wrap<float>(order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dgemm(int order, int TransA, int TransB, int M, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { gemm_wrap<double>(order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_ssymm(int order, int Side, int Uplo, int M, int N, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc) { symm_wrap<float>(order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dsymm(int order, int Side, int Uplo, int M, int N, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { symm_wrap<double>(order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_ssyrk(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, float beta, float *C, int ldc) { syrk_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
+ORACLE_API void oracle_dsyrk(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, double beta, double *C, int ldc) { syrk_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
+
+// ----- double-double high-precision references (results rounded to double)
+
+// Dot2 over strided windows (pointers already rebased by the caller).
+ORACLE_API double oracle_dd_dot(long n, const double *x, long incx, const double *y, long incy) {
+  DD acc{0.0, 0.0};
+  for (long i = 0; i < n; ++i) dd_add_prod(acc, x[i * incx], y[i * incy]);
+  DD r = dd_norm(acc);
+  return r.hi + r.lo;
+}
+
+// y_out[i] = alpha * sum_j op(A)[i,j] x[j] + beta * y_in[i] in double-double;
+// trans != 0 means op(A) = A^T.  m x n is the shape of op(A); A is row-major.
+ORACLE_API void oracle_dd_gemv(int trans, long m, long n, double alpha, const double *A, long lda, const double *x, double beta, const double *y_in, double *y_out) {
+  for (long i = 0; i < m; ++i) {
+    DD acc{0.0, 0.0};
+    for (long j = 0; j < n; ++j) dd_add_prod(acc, trans ? A[j * lda + i] : A[i * lda + j], x[j]);
+    DD r = dd_norm(acc);
+    // alpha * (hi + lo) + beta * y, each product exact-split then summed
+    DD out{0.0, 0.0};
+    dd_add_prod(out, alpha, r.hi);
+    dd_add_prod(out, alpha, r.lo);
+    dd_add_prod(out, beta, y_in[i]);
+    out = dd_norm(out);
+    y_out[i] = out.hi + out.lo;
+  }
+}
+
+// Forward/back substitution in double-double.  x holds b on entry (unit
+// stride) and the double-rounded solution on exit; x_lo receives the low
+// parts so callers can measure forward error below one ulp.
+ORACLE_API void oracle_dd_trsv(int uplo, int trans, int diag, long n, const double *A, long lda, double *x, double *x_lo) {
+  std::vector<DD> xs(n);
+  for (long i = 0; i < n; ++i) xs[i] = DD{x[i], 0.0};
+  auto at = [&](long r, long c) { return trans ? A[c * lda + r] : A[r * lda + c]; };
+  const bool lower_eff = (uplo == kLower) != (trans != 0);
+  for (long t = 0; t < n; ++t) {
+    const long i = lower_eff ? t : n - 1 - t;
+    DD acc{xs[i].hi, xs[i].lo};
+    const long j0 = lower_eff ? 0 : i + 1, j1 = lower_eff ? i : n;
+    for (long j = j0; j < j1; ++j) {
+      const double aij = at(i, j);
+      dd_add_prod(acc, -aij, xs[j].hi);
+      dd_add_prod(acc, -aij, xs[j].lo);
+    }
+    acc = dd_norm(acc);
+    if (diag == kNonUnit) {
+      // double-double divide by a double: q1 = hi/d, r = acc - q1*d, q2 = r/d
+      const double d = at(i, i);
+      double q1 = acc.hi / d;
+      double p, pe;
+      two_prod(q1, d, p, pe);
+      double r = ((acc.hi - p) - pe) + acc.lo;
+      double q2 = r / d;
+      double s, e;
+      two_sum(q1, q2, s, e);
+      acc = DD{s, e};
+    }
+    xs[i] = acc;
+  }
+  for (long i = 0; i < n; ++i) {
+    x[i] = xs[i].hi + xs[i].lo;
+    if (x_lo) x_lo[i] = (xs[i].hi - x[i]) + xs[i].lo;
+  }
+}
+
+// Selected entries of alpha * op(A) op(B) + beta * C in double-double:
+// out[t] for (rows[t], cols[t]), t < count.  op(A) is m x k, op(B) is k x n.
+ORACLE_API void oracle_dd_gemm_entries(int transa, int transb, long k, double alpha, const double *A, long lda, const double *B, long ldb, double beta, const double *C, long ldc, const long *rows, const long *cols, long count, double *out) {
+  for (long t = 0; t < count; ++t) {
+    const long i = rows[t], j = cols[t];
+    DD acc{0.0, 0.0};
+    for (long p = 0; p < k; ++p) {
+      const double a = transa ? A[p * lda + i] : A[i * lda + p];
+      const double b = transb ? B[j * ldb + p] : B[p * ldb + j];
+      dd_add_prod(acc, a, b);
+    }
+    DD r = dd_norm(acc);
+    DD o{0.0, 0.0};
+    dd_add_prod(o, alpha, r.hi);
+    dd_add_prod(o, alpha, r.lo);
+    if (C) dd_add_prod(o, beta, C[i * ldc + j]);
+    o = dd_norm(o);
+    out[t] = o.hi + o.lo;
+  }
+}
+
+// ----- multi-threaded drivers of the same algorithms (CPU baseline timing)
+
+ORACLE_API void oracle_par_saxpy(int nthreads, int N, float alpha, const float *X, float *Y) {
+  parallel_for(nthreads, N, [&](int, long lo, long hi) { oracle_saxpy((int)(hi - lo), alpha, X + lo, 1, Y + lo, 1); });
+}
+ORACLE_API void oracle_par_daxpy(int nthreads, int N, double alpha, const double *X, double *Y) {
+  parallel_for(nthreads, N, [&](int, long lo, long hi) { oracle_daxpy((int)(hi - lo), alpha, X + lo, 1, Y + lo, 1); });
+}
+ORACLE_API float oracle_par_sdot(int nthreads, int N, const float *X, const float *Y) {
+  std::vector<float> part(nthreads > 0 ? nthreads : 1, 0.0f);
+  parallel_for(nthreads, N, [&](int t, long lo, long hi) { part[t] = oracle_sdot((int)(hi - lo), X + lo, 1, Y + lo, 1); });
+  float r = 0.0f;
+  for (float p : part) r += p;
+  return r;
+}
+ORACLE_API double oracle_par_ddot(int nthreads, int N, const double *X, const double *Y) {
+  std::vector<double> part(nthreads > 0 ? nthreads : 1, 0.0);
+  parallel_for(nthreads, N, [&](int t, long lo, long hi) { part[t] = oracle_ddot((int)(hi - lo), X + lo, 1, Y + lo, 1); });
+  double r = 0.0;
+  for (double p : part) r += p;
+  return r;
+}
+ORACLE_API double oracle_par_dsdot(int nthreads, int N, const float *X, const float *Y) {
+  std::vector<double> part(nthreads > 0 ? nthreads : 1, 0.0);
+  parallel_for(nthreads, N, [&](int t, long lo, long hi) { part[t] = oracle_dsdot((int)(hi - lo), X + lo, 1, Y + lo, 1); });
+  double r = 0.0;
+  for (double p : part) r += p;
+  return r;
+}
+// y = beta*y + alpha*op(A) x with rows (NoTrans) or columns (Trans) of y split
+ORACLE_API void oracle_par_sgemv(int nthreads, int TransA, int M, int N, float alpha, const float *A, int lda, const float *X, float beta, float *Y) {
+  const long ylen = TransA == kNoTrans ? M : N;
+  parallel_for(nthreads, ylen, [&](int, long lo, long hi) {
+    if (TransA == kNoTrans)
+      oracle_sgemv(kRowMajor, kNoTrans, (int)(hi - lo), N, alpha, A + lo * lda, lda, X, 1, beta, Y + lo, 1);
+    else
+      oracle_sgemv(kRowMajor, TransA, M, (int)(hi - lo), alpha, A + lo, lda, X, 1, beta, Y + lo, 1);
+  });
+}
+// Blocked lower/no-trans solve: the off-diagonal panel of each 256-row block is
+// a parallel row-dot over the already solved prefix (trsv.py:31-36 per row),
+// the 256 x 256 diagonal block runs the proc sequentially.
+ORACLE_API void oracle_par_dtrsv_lnn(int nthreads, int N, const double *A, int lda, double *X) {
+  const long B = 256;
+  for (long k0 = 0; k0 < N; k0 += B) {
+    const long k1 = k0 + B < N ? k0 + B : N;
+    parallel_for(nthreads, k1 - k0, [&](int, long lo, long hi) {
+      for (long i = k0 + lo; i < k0 + hi; ++i) {
+        double dot = 0.0;
+        const double *ai = A + i * lda;
+        for (long j = 0; j < k0; ++j) dot += ai[j] * X[j];
+        X[i] -= dot;
+      }
+    });
+    oracle_dtrsv(kRowMajor, kLower, kNoTrans, kNonUnit, (int)(k1 - k0), A + k0 * lda + k0, lda, X + k0, 1);
+  }
+}
+ORACLE_API void oracle_par_sgemm(int nthreads, int TransA, int TransB, int M, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc) {
+  Mat<float> a{const_cast<float *>(A), lda}, b{const_cast<float *>(B), ldb}, c{C, ldc};
+  parallel_for(nthreads, M, [&](int, long lo, long hi) {
+    mscal_proc<float>(hi - lo, N, beta, Mat<float>{C + lo * ldc, ldc});
+    gemm_rows<float>(TransA, TransB, lo, hi, N, K, alpha, a, b, c);
+  });
+}

@@ -1,0 +1,48 @@
+"""Level-3 parity on the GPU (grids of test/level3/{gemm,symm,syrk}/correctness.cpp)."""
+import numpy as np
+import pytest
+
+from cases import gemm_cases, symm_cases, syrk_cases
+from common import EPS, check_case, run_gpu
+
+GEMM = [c for p in "sd" for c in gemm_cases(p)]
+SYMM = [c for p in "sd" for c in symm_cases(p)]
+SYRK = [c for p in "sd" for c in syrk_cases(p)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", GEMM, ids=lambda c: f"{c.op}-{c.label}")
+def test_gemm(cuda, case):
+    r, a = run_gpu(case)
+    check_case(case, r, a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", SYMM, ids=lambda c: f"{c.op}-{c.label}")
+def test_symm(cuda, case):
+    r, a = run_gpu(case)
+    check_case(case, r, a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", SYRK, ids=lambda c: f"{c.op}-{c.label}")
+def test_syrk(cuda, case):
+    r, a = run_gpu(case)
+    check_case(case, r, a)
+
+
+@pytest.mark.gpu
+def test_sgemm_config_1024(cuda):
+    """Config: sgemm NN 1024^3, lda=ldb=ldc=1024, alpha 1, beta 0.5, U[-1,1) seed 0."""
+    import exoblas_gb300 as eb
+
+    g = np.random.default_rng(0)
+    n = 1024
+    A = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    B = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    C = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    out = C.copy()
+    eb.exo_sgemm(101, 111, 111, n, n, n, 1.0, A, n, B, n, 0.5, out, n)
+    ref = A.astype(np.float64) @ B.astype(np.float64) + 0.5 * C.astype(np.float64)
+    mag = np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64)) + 0.5 * np.abs(C.astype(np.float64))
+    assert np.all(np.abs(out - ref) <= 4 * n * EPS["s"] * mag)
