@@ -79,6 +79,7 @@ EXTRA = {
     "exoblas_set_precision": ("i", "i"),
     "exoblas_get_precision": ("i", ""),
     "exoblas_kernel_launches": ("u", ""),
+    "exoblas_staged_bytes": ("v", "pp"),
     "exoblas_sasum_device": ("i", "ipip"),
     "exoblas_dasum_device": ("i", "ipip"),
     "exoblas_sdot_device": ("i", "ipipip"),

@@ -53,6 +53,7 @@ struct Context {
   bool own_stream = false;
   bool blocking = true;
   int precision = EXOBLAS_PRECISION_NATIVE;
+  bool status_pending = false;  // a kernel with bounded waits was queued
   Arena scratch;      // partial sums, flags, counters (zeroed regions noted per kernel)
   Arena counters;     // small zero-initialised words; kernels leave them zero
   Arena staging[6];   // device copies of host operands, one slot per operand

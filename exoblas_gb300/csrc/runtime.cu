@@ -14,6 +14,7 @@
 namespace exb {
 
 static std::atomic<unsigned long long> g_launches{0};
+static std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
 void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 static thread_local int tl_status = EXOBLAS_SUCCESS;
@@ -158,6 +159,7 @@ void *Stager::stage(const void *p, size_t elem, long count, long inc, bool out) 
   s = Slot{const_cast<char *>(base), d, bytes, 0, 0, 0, out};
   any_host = true;
   h2d += bytes;
+  g_h2d.fetch_add(bytes, std::memory_order_relaxed);
   return d - lo * long(elem);
 }
 
@@ -176,6 +178,7 @@ void *Stager::stage_matrix(const void *p, size_t elem, long rows, long cols, lon
   s = Slot{const_cast<void *>(p), d, bytes, pitch, width, size_t(rows), out};
   any_host = true;
   h2d += size_t(rows) * width;
+  g_h2d.fetch_add(size_t(rows) * width, std::memory_order_relaxed);
   return d;
 }
 
@@ -183,6 +186,7 @@ void Stager::finish() {
   for (int i = 0; i < nslots; ++i) {
     Slot &s = slots[i];
     if (!s.out) continue;
+    g_d2h.fetch_add(s.rows ? s.rows * s.width : s.bytes, std::memory_order_relaxed);
     if (s.rows) {
       // matrices: copy back only the rows' used columns so padding between
       // rows (ld > cols) is never written
@@ -195,13 +199,33 @@ void Stager::finish() {
       EXB_CUDA(cudaMemcpyAsync(s.host, s.dev, s.bytes, cudaMemcpyDeviceToHost, c.stream));
     }
   }
-  if (any_host || c.blocking) EXB_CUDA(cudaStreamSynchronize(c.stream));
+  if (any_host || c.blocking) {
+    EXB_CUDA(cudaStreamSynchronize(c.stream));
+    check_device_status();
+  }
 }
 
 // Device status word written by kernels with bounded waits.
 int *device_status_word() { return reinterpret_cast<int *>(zero_words(64) + 32); }
 
 void set_status(int s) { tl_status = s; }
+
+// Reads (after the caller synchronised the stream) and clears the device
+// status word; a nonzero value means a bounded wait ran out.
+void check_device_status() {
+  Context &c = ctx();
+  if (!c.status_pending) return;
+  c.status_pending = false;
+  int st = 0;
+  int *w = device_status_word();
+  EXB_CUDA(cudaMemcpyAsync(&st, w, 4, cudaMemcpyDeviceToHost, c.stream));
+  EXB_CUDA(cudaStreamSynchronize(c.stream));
+  if (st) {
+    EXB_CUDA(cudaMemsetAsync(w, 0, 4, c.stream));
+    EXB_CUDA(cudaStreamSynchronize(c.stream));
+    fail(EXOBLAS_TIMEOUT, "a kernel's bounded wait ran out");
+  }
+}
 
 void report(int status, const char *fn, const char *msg) {
   tl_status = status;
@@ -257,7 +281,10 @@ int exoblas_set_blocking(int b) {
 }
 
 int exoblas_synchronize(void) {
-  return guarded("exoblas_synchronize", [&] { EXB_CUDA(cudaStreamSynchronize(ctx().stream)); });
+  return guarded("exoblas_synchronize", [&] {
+    EXB_CUDA(cudaStreamSynchronize(ctx().stream));
+    check_device_status();
+  });
 }
 
 int exoblas_set_precision(int mode) {
@@ -275,5 +302,10 @@ int exoblas_get_precision(void) {
 }
 
 unsigned long long exoblas_kernel_launches(void) { return g_launches.load(); }
+
+void exoblas_staged_bytes(unsigned long long *h2d, unsigned long long *d2h) {
+  if (h2d) *h2d = g_h2d.load();
+  if (d2h) *d2h = g_d2h.load();
+}
 
 }  // extern "C"

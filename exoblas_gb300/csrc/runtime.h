@@ -16,6 +16,9 @@ void report(int status, const char *fn, const char *msg);
 // Device word (in the zeroed counter region) where kernels with bounded
 // waits record a timeout; the host reads and clears it after the call.
 int *device_status_word();
+// After a stream synchronisation: raises EXOBLAS_TIMEOUT if a kernel queued
+// since the last check recorded an expired wait (see Context::status_pending).
+void check_device_status();
 
 // Runs `body`, converting library errors into the thread's status.  Returns
 // the status (0 on success).

@@ -154,27 +154,24 @@ void trsv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x,
   if (n <= 0) return;
   Context &c = ctx();
   const long nb = ceil_div(n, kB);
-  // scratch: contiguous z, nb flags, ticket
-  const size_t zbytes = (size_t(n) * sizeof(T) + 255) & ~size_t(255);
+  // scratch: contiguous z (only when x is strided), nb flags, ticket
+  const bool inplace = incx == 1;
+  const size_t zbytes = inplace ? 0 : (size_t(n) * sizeof(T) + 255) & ~size_t(255);
   char *base = static_cast<char *>(scratch(zbytes + size_t(nb + 1) * 4));
-  T *z = reinterpret_cast<T *>(base);
+  T *z = inplace ? x : reinterpret_cast<T *>(base);
   int *flags = reinterpret_cast<int *>(base + zbytes);
   int *ticket = flags + nb;
   int *status = device_status_word();
   EXB_CUDA(cudaMemsetAsync(flags, 0, size_t(nb + 1) * 4, c.stream));
-  l1::copy<T>(n, x, incx, z, 1);
+  if (!inplace) l1::copy<T>(n, x, incx, z, 1);
   int blocks = int(nb < grid_cap(4) ? nb : grid_cap(4));
   trsv_kernel<T><<<blocks, kTThreads, 0, c.stream>>>(n, A, lda, z, upper != trans, trans, unit, flags, ticket, status);
   EXB_LAUNCH("trsv kernel");
   count_launch();
-  l1::copy<T>(n, z, 1, x, incx);
-  int st = 0;
-  EXB_CUDA(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, c.stream));
-  EXB_CUDA(cudaStreamSynchronize(c.stream));
-  if (st) {
-    EXB_CUDA(cudaMemsetAsync(status, 0, 4, c.stream));
-    fail(EXOBLAS_TIMEOUT, "trsv: a block-ready wait ran out");
-  }
+  if (!inplace) l1::copy<T>(n, z, 1, x, incx);
+  // the timeout flag is read at the call's final synchronisation (blocking
+  // mode) or by exoblas_synchronize()
+  c.status_pending = true;
 }
 
 template void trsv<float>(bool, bool, bool, long, const float *, long, float *, long);

@@ -77,6 +77,8 @@ EXOBLAS_API void *exoblas_get_stream(void);
  * (asum, dot, dsdot, sdsdot) still wait for their result.  Use the
  * exoblas_*_device variants below for fully asynchronous reductions. */
 EXOBLAS_API int exoblas_set_blocking(int blocking);
+/* Waits for the thread's queued work.  Also reports EXOBLAS_TIMEOUT when a
+ * kernel queued in non-blocking mode (trsv) gave up a bounded wait. */
 EXOBLAS_API int exoblas_synchronize(void);
 
 /* Arithmetic used by exo_sgemm/ssymm/ssyrk and exo_dgemm:
@@ -94,6 +96,9 @@ EXOBLAS_API int exoblas_get_precision(void);
 
 /* Number of CUDA kernels this library has launched in the calling process. */
 EXOBLAS_API unsigned long long exoblas_kernel_launches(void);
+/* Bytes this process has copied host->device and device->host while staging
+ * host operands (no counterpart in the reference, which has no device). */
+EXOBLAS_API void exoblas_staged_bytes(unsigned long long *h2d, unsigned long long *d2h);
 
 /* ------------------------------------------------------------ level 1 --- */
 /* test/level1/asum/exo_asum_wrapper.h:5-23 (incX < 0 returns 0) */
