@@ -311,6 +311,7 @@ def main():
 
     X = make_inputs(torch, f"cuda:{local}")
     res = torch.zeros(8, dtype=torch.float64, device=f"cuda:{local}")
+    torch.cuda.synchronize()  # inputs were generated on the default stream
     run = launchers(L, X, res)
     names = [k for k, _ in KERNELS]
 

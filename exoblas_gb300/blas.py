@@ -23,6 +23,7 @@ CblasNonUnit, CblasUnit = 131, 132
 CblasLeft, CblasRight = 141, 142
 
 PRECISION_NATIVE, PRECISION_SPLIT_BF16, PRECISION_OZAKI = 0, 1, 2
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy
 
 
 class ExoBlasError(RuntimeError):
@@ -55,11 +56,14 @@ def _ptr(a):
         if a.is_cuda:
             import torch
 
-            s = torch.cuda.current_stream(a.device).cuda_stream
+            # torch's default stream is the legacy default stream (handle 0);
+            # the library takes it as cudaStreamLegacy (0x1), NULL meaning the
+            # library's own stream
+            s = torch.cuda.current_stream(a.device).cuda_stream or CUDA_STREAM_LEGACY
             if s != _torch_stream:
                 # run this library's kernels on torch's current stream so they
                 # are ordered after the kernels that produced the tensors
-                _native.lib().exoblas_set_stream(s or None)
+                _native.lib().exoblas_set_stream(s)
                 _torch_stream = s
         return a.data_ptr()
     if hasattr(a, "__array_interface__"):
@@ -112,10 +116,17 @@ def set_blocking(blocking: bool) -> None:
 
 
 def set_stream(stream) -> None:
-    """Use a CUDA stream (torch.cuda.Stream, raw handle or None) for this thread's calls."""
+    """Use a CUDA stream for this thread's calls: a torch.cuda.Stream (its
+    default stream maps to cudaStreamLegacy), a raw cudaStream_t handle, or
+    None for the library's own non-blocking stream."""
     global _torch_stream
-    handle = getattr(stream, "cuda_stream", stream)
-    _native.lib().exoblas_set_stream(handle or None)
+    if stream is None:
+        handle = None
+    elif hasattr(stream, "cuda_stream"):
+        handle = stream.cuda_stream or CUDA_STREAM_LEGACY
+    else:
+        handle = int(stream)
+    _native.lib().exoblas_set_stream(handle)
     _check("exoblas_set_stream")
     _torch_stream = handle
 

@@ -66,7 +66,9 @@ EXOBLAS_API void exoblas_set_error_handler(exoblas_error_handler handler);
 
 /* ------------------------------------------------------ execution state - */
 /* Stream used by the calling thread's subsequent calls on the current device
- * (a cudaStream_t; NULL selects the library's own non-blocking stream).
+ * (a cudaStream_t, including cudaStreamLegacy / cudaStreamPerThread; NULL
+ * selects the library's own non-blocking stream, which is not ordered with
+ * the legacy default stream).
  * Work already queued by this thread on its previous stream is synchronised
  * first, so scratch memory is never shared by two streams at once. */
 EXOBLAS_API int exoblas_set_stream(void *stream);
