@@ -85,6 +85,7 @@ EXTRA = {
     "exoblas_sdot_device": ("i", "ipipip"),
     "exoblas_ddot_device": ("i", "ipipip"),
     "exoblas_dsdot_device": ("i", "ipipip"),
+    "exoblas_sgemv_noalloc": ("i", "iiiifpipifpip"),
 }
 
 SIGNATURES = {**L1, **L2, **L3, **EXTRA}

@@ -178,6 +178,26 @@ EXOBLAS_API void exo_strsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO U
 EXOBLAS_API void exo_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX);
 
+/* exoblas_sgemv_noalloc: no counterpart in the reference.  exo_sgemv for
+ * callers that cannot allocate device memory (e.g. a plugin inside a
+ * framework whose allocator owns all device memory, or a loop that must not
+ * block in the driver's allocator).  Same arguments and arithmetic as
+ * exo_sgemv plus a cudaStream_t (NULL: the legacy default stream); A, X and Y
+ * must be device pointers.  The call queues its kernels and returns without
+ * waiting, and returns the status (also readable with exoblas_get_status).
+ * It allocates nothing: its scratch is a fixed 4 MiB array inside the
+ * library, held on every GPU that loads it.  Limit: a Trans call needs
+ * 4*N bytes (one column-sum chunk) plus, when X is strided or not 16-byte
+ * aligned, 4*M bytes for a packed copy of X; a NoTrans call with such an X
+ * needs 4*N bytes; larger problems are rejected with EXOBLAS_INVALID_VALUE
+ * before any work is queued.  Every call shares the array, so calls that
+ * overlap on the GPU race and must be serialised.  The first call on each
+ * device looks the array's address up (cudaGetSymbolAddress); make it before
+ * any stream capture starts on that device. */
+EXOBLAS_API int exoblas_sgemv_noalloc(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M,
+                                      const int N, const float alpha, const float *A, const int lda, const float *X,
+                                      const int incX, const float beta, float *Y, const int incY, void *stream);
+
 /* ------------------------------------------------------------ level 3 --- */
 /* test/level3/gemm/exo_gemm_wrapper.h:9-28 (C *= beta, then C += alpha op(A) op(B)) */
 EXOBLAS_API void exo_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
