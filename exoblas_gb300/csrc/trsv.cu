@@ -25,6 +25,7 @@ namespace l2 {
 constexpr int kB = 64;
 constexpr int kTThreads = 256;
 constexpr long long kSpinLimit = 1ll << 24;  // ~ seconds with the back-off below
+constexpr long kClusterMinN = 192;            // from here on the clustered solver is used
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
   int v;
@@ -150,8 +151,13 @@ __global__ void __launch_bounds__(kTThreads)
 }
 
 template <typename T>
+bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x);
+
+template <typename T>
 void trsv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx) {
   if (n <= 0) return;
+  // large contiguous solves: the clustered solver (trsv_cluster.cu)
+  if (incx == 1 && n >= kClusterMinN && trsv_cluster<T>(upper, trans, unit, n, A, lda, x)) return;
   Context &c = ctx();
   const long nb = ceil_div(n, kB);
   // scratch: contiguous z (only when x is strided), nb flags, ticket

@@ -1,0 +1,588 @@
+// Triangular solve (src/level2/trsv.py:10-52) for large n: blocked
+// substitution in one persistent launch of 8-CTA thread-block clusters.
+//
+// Effective-lower formulation as in trsv.cu: L(i, j) = trans ? A[c(j)][c(i)]
+// : A[c(i)][c(j)], c(k) = rev ? n-1-k : k, z = x in effective order.  Blocks
+// of kTB = 64 rows.  Roles, decided at run time so that the solver is always
+// a cluster that is already running:
+//
+//  * the first cluster to start is the SOLVER.  CTA r of it owns rows
+//    [8r, 8r+8) of every block.  Step K: rhs = b_K - (bulk partial sums of
+//    block row K) - L[K,K-2] x_{K-2} - L[K,K-1] x_{K-1}, exchanged between
+//    the 8 CTAs through distributed shared memory, then x_K = inv(L_KK) rhs
+//    (the diagonal block solved in shared memory with its inverse, computed
+//    beforehand by trsv_inverse_kernel in the working precision), exchanged
+//    again and published to global memory with a release flag.  Everything
+//    except the L[K,K-1] product and the two exchanges is done in the
+//    shadow of the previous step's cluster barrier, and the operand rows the
+//    solver needs are prefetched kPre steps ahead with cp.async.
+//  * every other CTA STREAMS the bulk: work items (K, c) cover tiles
+//    L[K, J] for J in chunk c (kCT tiles) with J < K - kD, claimed in order of
+//    K (the step that needs them) through an atomic ticket.  An item writes
+//    its 64 partial row sums to slot (K, c) and sets the slot's flag; the
+//    solver adds the slots of block row K in slot order, so results are
+//    deterministic.
+//
+// Deadlock freedom: the solver only waits on items, which are claimed in
+// order by running CTAs and themselves only wait on the solver's x flags;
+// streamers only wait on the solver, which is running.  Every wait is
+// bounded: on expiry the CTA records the timeout in the device status word,
+// stops waiting for the rest of the launch, and the host reports
+// EXOBLAS_TIMEOUT.  Solver CTAs keep arriving at every cluster barrier so the
+// cluster always completes.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace cg = cooperative_groups;
+
+namespace exb {
+namespace l2 {
+
+namespace tc {
+
+constexpr int kTB = 64;            // block size
+constexpr int kNT = 256;           // threads per CTA
+constexpr int kCT = 8;             // tiles per streamer chunk
+constexpr int kD = 6;              // near tiles done by the solver: J = K-1 .. K-kD
+constexpr int kPre = 4;            // solver prefetch depth (steps)
+constexpr int kXR = 8;             // x ring depth (>= kD + 1)
+constexpr long long kSpin = 1ll << 24;
+
+template <typename T>
+struct SmemStream {
+  T tile[2][kTB][kTB + 1];
+  T zs[kCT][kTB];
+};
+
+template <typename T>
+struct Args {
+  long n;
+  const T *A;
+  long lda;
+  T *z;
+  const T *inv;  // nb x kTB x kTB
+  T *slots;      // nb x nch x kTB
+  int *xflag;    // nb
+  int *sflag;    // nb x nch
+  int *ctl;      // [0] solver claim, [1] item ticket
+  int *status;
+  int nb, nch;
+  bool rev, trans, unit;
+};
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+template <typename T>
+__device__ __forceinline__ void cp_async(T *smem, const T *gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// global index of effective element L(i, j) (both < n); A row-major
+template <typename T>
+__device__ __forceinline__ long lidx(const Args<T> &a, long i, long j) {
+  const long ci = a.rev ? a.n - 1 - i : i, cj = a.rev ? a.n - 1 - j : j;
+  return a.trans ? cj * a.lda + ci : ci * a.lda + cj;
+}
+template <typename T>
+__device__ __forceinline__ long zidx(const Args<T> &a, long i) {
+  return a.rev ? a.n - 1 - i : i;
+}
+
+// Bounded wait for *p != 0 by thread 0; returns false (and records the
+// timeout) when it expires.
+__device__ __forceinline__ bool wait_flag(const int *p, int *status, bool &dead) {
+  if (dead) return false;
+  long long spins = 0;
+  while (ld_acquire(p) == 0) {
+    if (++spins > kSpin) {
+      atomicExch(status, 1);
+      dead = true;
+      return false;
+    }
+    __nanosleep(64);
+  }
+  return true;
+}
+
+// number of bulk chunks of block row K, and items before row K
+__device__ __host__ __forceinline__ int nch_row(long K) { return K > kD ? int((K - kD + kCT - 1) / kCT) : 0; }
+__device__ __host__ __forceinline__ long items_before(long K) {
+  const long M = K - 1 - kD;
+  if (M <= 0) return 0;
+  const long q = M / kCT, r = M % kCT;
+  return kCT * q * (q + 1) / 2 + r * (q + 1);
+}
+
+// ------------------------------------------------------------ streamers ----
+template <typename T>
+__device__ void stream_items(const Args<T> &a, SmemStream<T> &S, bool &dead) {
+  __shared__ long s_item;
+  const int tid = threadIdx.x;
+  const long total = items_before(a.nb);
+  const int i = tid >> 2, q = tid & 3;  // row, quarter of the tile product
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_item = atomicAdd(a.ctl + 1, 1);
+    __syncthreads();
+    const long t = s_item;
+    if (t >= total) return;
+    // item t -> (K, c): largest K with items_before(K) <= t
+    long lo = kD + 1, hi = a.nb - 1;
+    while (lo < hi) {
+      const long mid = (lo + hi + 1) / 2;
+      if (items_before(mid) <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const long K = lo;
+    const int c = int(t - items_before(K));
+    const long J0 = long(c) * kCT;
+    long J1 = J0 + kCT;
+    if (J1 > K - kD) J1 = K - kD;
+    const int ntiles = int(J1 - J0);
+    // stage tile J0 (and J0+1) with cp.async; element (r, cc) = L(K*64+r, J*64+cc)
+    auto issue = [&](int slot, long J) {
+      for (int e = tid; e < kTB * kTB; e += kNT) {
+        // consecutive threads walk along A's contiguous dimension
+        const int r = a.trans ? e % kTB : e / kTB, cc = a.trans ? e / kTB : e % kTB;
+        const long gi = K * kTB + r, gj = J * kTB + cc;
+        if (gi < a.n && gj < a.n)
+          cp_async(&S.tile[slot][r][cc], a.A + lidx(a, gi, gj));
+        else
+          S.tile[slot][r][cc] = T(0);
+      }
+      cp_commit();
+    };
+    T acc = 0;
+    issue(0, J0);
+    for (int tt = 0; tt < ntiles; ++tt) {
+      const long J = J0 + tt;
+      if (tt + 1 < ntiles) issue((tt + 1) & 1, J + 1);
+      else cp_commit();  // keep one group per iteration
+      // x_J must be published by the solver
+      if (tid == 0) wait_flag(a.xflag + J, a.status, dead);
+      __syncthreads();
+      if (tid < kTB) {
+        const long gj = J * kTB + tid;
+        S.zs[tt][tid] = gj < a.n ? __ldcg(a.z + zidx(a, gj)) : T(0);
+      }
+      cp_wait<1>();
+      __syncthreads();
+      const int slot = tt & 1;
+#pragma unroll
+      for (int jj = 0; jj < kTB / 4; ++jj) {
+        const int j = q * (kTB / 4) + jj;
+        acc = fma(S.tile[slot][i][j], S.zs[tt][j], acc);
+      }
+      __syncthreads();
+    }
+    cp_wait<0>();
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (q == 0) a.slots[(K * a.nch + c) * kTB + i] = acc;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(a.sflag + K * a.nch + c, 1);
+  }
+}
+
+// --------------------------------------------------------------- solver ----
+// Solver cluster of CS CTAs; CTA r owns rows [r*RPC, (r+1)*RPC) of every
+// block.  Per step K the critical path is: t0 = L[K,K-1] x_{K-1} for the
+// owned rows -> residual exchange -> x_K = inv(L_KK) r -> x exchange.  All
+// other work for step K+1 (the near tiles L[K+1, K+1-j] x_{K+1-j} for
+// j = 2..kD, which only need x values already known, and the bulk slot sums)
+// runs in the shadows of the two cluster barriers.
+template <typename T, int CS>
+struct SmemSolver {
+  static constexpr int RPC = kTB / CS;
+  static constexpr int kStage = (kD + 1) * RPC * kTB;  // near tiles j = 0..kD-1, then inv rows
+  T stage[kPre][kStage];
+  T bvals[kPre][RPC];
+  T rfull[2][kTB];
+  T xring[kXR][kTB];
+  T nearres[2][RPC];  // shadow near-tile sums per row (one or two warps per row)
+  T carry[RPC];
+};
+
+template <typename T, int CS>
+__device__ void solve_chain(const Args<T> &a, SmemSolver<T, CS> &S, bool &dead) {
+  constexpr int RPC = kTB / CS;
+  constexpr int kStage = SmemSolver<T, CS>::kStage;
+  cg::cluster_group cl = cg::this_cluster();
+  const int R = int(cl.block_rank());
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long n = a.n;
+  const int nb = a.nb;
+
+  // stage K: near tile j (L[K, K-1-j]) rows at j*RPC*kTB, inv rows at kD*RPC*kTB
+  auto prefetch = [&](long K) {
+    if (K < nb) {
+      T *st = S.stage[K % kPre];
+      for (int e = tid; e < kStage; e += kNT) {
+        const int which = e / (RPC * kTB), rem = e % (RPC * kTB);
+        const int r = rem / kTB, cc = rem % kTB;
+        const long gi = K * kTB + R * RPC + r;
+        if (which < kD) {
+          const long J = K - 1 - which;
+          const long gj = J * kTB + cc;
+          if (J >= 0 && gi < n && gj < n)
+            cp_async(st + e, a.A + lidx(a, gi, gj));
+          else
+            st[e] = T(0);
+        } else {
+          cp_async(st + e, a.inv + (K * kTB + R * RPC + r) * kTB + cc);
+        }
+      }
+      if (tid < RPC) {
+        const long gi = K * kTB + R * RPC + tid;
+        if (gi < n)
+          cp_async(&S.bvals[K % kPre][tid], a.z + zidx(a, gi));
+        else
+          S.bvals[K % kPre][tid] = T(0);
+      }
+    }
+    cp_commit();
+  };
+  // Measured on GB300: one warp issues at most one FP64 instruction per ~64
+  // clocks and a shuffle + FP64 add step costs ~100 clocks, while the SM's
+  // FP64 pipe takes a warp instruction every ~19 clocks once 4+ warps issue.
+  // So FP64 work is spread one row per warp with short dependency chains.
+  // rowdot: one warp, row `row` (64 entries) . v; result in every lane
+  auto rowdot = [&](const T *row, const T *v) -> T {
+    T s = fma(row[lane + 32], v[lane + 32], row[lane] * v[lane]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+  };
+  constexpr int kWPR = (kNT / 32) / RPC;  // warps per owned row in the shadows (1 or 2)
+  // lanes c < nc of the row-owner warps hold slot values of the next row
+  T pend = 0;
+  int pend_nc = 0;
+  // warp 0 polls the slot flags of block row K2, then the row-owner warps
+  // load the slot values into `pend` (used one step later)
+  auto request_slots = [&](long K2) {
+    pend = 0;
+    pend_nc = 0;
+    if (K2 >= nb) return;
+    const int nc = nch_row(K2);
+    if (nc == 0) return;
+    if (warp == 0 && !dead) {
+      long long spins = 0;
+      for (;;) {
+        int ok = 1;
+        for (int cc = lane; cc < nc; cc += 32) ok &= ld_acquire(a.sflag + K2 * a.nch + cc) != 0;
+        if (__all_sync(0xffffffffu, ok)) break;
+        if (++spins > kSpin) {
+          if (lane == 0) atomicExch(a.status, 1);
+          dead = true;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __syncthreads();
+    pend_nc = nc;
+    // lane c of row warp w sums slots c, c+32, ... of row w (the loads
+    // complete during the next step)
+    if (warp < RPC) {
+      T v = 0;
+      for (int cc = lane; cc < nc; cc += 32) v += __ldcg(a.slots + (K2 * a.nch + cc) * kTB + R * RPC + warp);
+      pend = v;
+    }
+  };
+
+  for (int p = 0; p < kPre; ++p) prefetch(p);
+  if (tid < RPC) S.carry[tid] = T(0);
+  // bulk of rows 0 and 1 is empty (nch_row(K) = 0 for K <= kD)
+  request_slots(1);
+  for (long K = 0; K < nb; ++K) {
+    const int sidx = int(K % kPre);
+    cp_wait<kPre - 1>();
+    __syncthreads();
+    const T *st = S.stage[sidx];
+    // ---- critical: residual of the owned rows
+    if (warp < RPC) {
+      const T t0 = K >= 1 ? rowdot(st + warp * kTB, S.xring[(K - 1) % kXR]) : T(0);
+      const T rr = S.bvals[sidx][warp] - S.carry[warp] - t0;
+      // lane d writes the residual to CTA d
+      if (lane < CS) *cl.map_shared_rank(&S.rfull[K & 1][R * RPC + warp], lane) = rr;
+    }
+    cluster_arrive();
+    // ---- shadow 1: near tiles j = 1..kD-1 of step K+1 (x_{K-1} .. x_{K+1-kD})
+    // and publishing x_{K-1} to global memory for the streamers
+    if (K + 1 < nb) {
+      cp_wait<kPre - 2>();
+      __syncthreads();
+      const T *st1 = S.stage[(K + 1) % kPre];
+      // warp w: row w % RPC, near tiles j = 1 + w / RPC, 1 + w / RPC + kWPR, ...
+      {
+        const int r = warp % RPC, j0 = 1 + warp / RPC;
+        T s0 = 0, s1 = 0;
+        for (int j = j0; j < kD; j += kWPR) {
+          const long J = K - j;
+          if (J < 0) break;
+          const T *row = st1 + (j * RPC + r) * kTB;
+          const T *xv = S.xring[J % kXR];
+          s0 = fma(row[lane], xv[lane], s0);
+          s1 = fma(row[lane + 32], xv[lane + 32], s1);
+        }
+        T sum = s0 + s1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) S.nearres[warp / RPC][r] = sum;
+      }
+    }
+    if (R == 0 && K >= 1 && warp == RPC - 1 + (RPC < kNT / 32 ? 1 : 0)) {
+      // publish x_{K-1}: the last warp writes it, fences and raises the flag
+      for (int t = lane; t < kTB; t += 32) {
+        const long gi = (K - 1) * kTB + t;
+        if (gi < n) a.z[zidx(a, gi)] = S.xring[(K - 1) % kXR][t];
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release(a.xflag + K - 1, 1);
+    }
+    cluster_wait();
+    // ---- critical: x_K rows = inv(L_KK)[rows] . rfull
+    if (warp < RPC) {
+      const T xk = rowdot(st + (kD * RPC + warp) * kTB, S.rfull[K & 1]);
+      if (lane < CS) *cl.map_shared_rank(&S.xring[K % kXR][R * RPC + warp], lane) = xk;
+    }
+    cluster_arrive();
+    // ---- shadow 2: refill stage K, carry for step K+1, slot loads for K+2
+    __syncthreads();
+    prefetch(K + kPre);
+    if (warp < RPC) {
+      T b = pend_nc > 0 ? pend : T(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) b += __shfl_xor_sync(0xffffffffu, b, o);
+      if (lane == 0) {
+        T nr = S.nearres[0][warp];
+        if (kWPR > 1) nr += S.nearres[1][warp];
+        S.carry[warp] = (K + 1 < nb) ? b + nr : T(0);
+      }
+    }
+    request_slots(K + 2);
+    cluster_wait();
+  }
+  // publish the last block
+  if (R == 0 && warp == RPC - 1 + (RPC < kNT / 32 ? 1 : 0)) {
+    for (int t = lane; t < kTB; t += 32) {
+      const long gi = (nb - 1) * long(kTB) + t;
+      if (gi < n) a.z[zidx(a, gi)] = S.xring[(nb - 1) % kXR][t];
+    }
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) st_release(a.xflag + nb - 1, 1);
+  }
+  cp_wait<0>();
+}
+
+template <typename T, int CS>
+__global__ void __launch_bounds__(kNT, 1) trsv_cluster_kernel(Args<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ int s_role;
+  // role: rank 0 of each cluster tries to claim the solver role
+  if (threadIdx.x == 0) s_role = 0;
+  if (cl.block_rank() == 0 && threadIdx.x == 0) s_role = atomicCAS(a.ctl, 0, 1) == 0 ? 1 : 0;
+  cl.sync();
+  const int role = *cl.map_shared_rank(&s_role, 0);
+  cl.sync();
+  bool dead = false;
+  if (role == 1)
+    solve_chain<T, CS>(a, *reinterpret_cast<SmemSolver<T, CS> *>(smem_raw), dead);
+  else
+    stream_items<T>(a, *reinterpret_cast<SmemStream<T> *>(smem_raw), dead);
+}
+
+// ------------------------------------------------- diagonal-block inverse --
+// inv[K] = inverse of the effective lower-triangular diagonal block L_KK
+// (unit diagonal when `unit`; rows/columns beyond n are the identity).
+// Column c of the inverse is y with L y = e_c: y_c = 1/L_cc,
+// y_i = -(sum_{j=c}^{i-1} L_ij y_j) * (1/L_ii); four lanes share a column.
+// The reciprocals of the diagonal are formed once (64 divisions per block):
+// an FP64 division per element is far too slow on this FP64 pipe.
+template <typename T>
+__global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
+  __shared__ T L[kTB][kTB + 1];
+  __shared__ T Y[kTB][kTB + 1];  // Y[i][c]
+  __shared__ T rd[kTB];
+  const long K = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kTB * kTB; e += kNT) {
+    const int r = a.trans ? e % kTB : e / kTB, cc = a.trans ? e / kTB : e % kTB;
+    const long gi = K * kTB + r, gj = K * kTB + cc;
+    T v;
+    if (gi < a.n && gj < a.n)
+      v = cc <= r ? a.A[lidx(a, gi, gj)] : T(0);
+    else
+      v = r == cc ? T(1) : T(0);
+    if (r == cc && (a.unit || gi >= a.n)) v = T(1);
+    L[r][cc] = v;
+    Y[r][cc] = T(0);
+  }
+  __syncthreads();
+  if (tid < kTB) rd[tid] = T(1) / L[tid][tid];
+  __syncthreads();
+  const int c = tid >> 2, q = tid & 3;
+  const unsigned mask = 0xfu << ((threadIdx.x & 31) & ~3);
+  if (q == 0) Y[c][c] = rd[c];
+  __syncwarp(mask);
+  for (int i = c + 1; i < kTB; ++i) {
+    T s0 = 0, s1 = 0;
+    int j = c + q;
+    for (; j + 4 < i; j += 8) {
+      s0 = fma(L[i][j], Y[j][c], s0);
+      s1 = fma(L[i][j + 4], Y[j + 4][c], s1);
+    }
+    if (j < i) s0 = fma(L[i][j], Y[j][c], s0);
+    T s = s0 + s1;
+    s += __shfl_xor_sync(mask, s, 1);
+    s += __shfl_xor_sync(mask, s, 2);
+    if (q == 0) Y[i][c] = -s * rd[i];
+    __syncwarp(mask);
+  }
+  __syncthreads();
+  T *out = const_cast<T *>(a.inv) + K * kTB * kTB;
+  for (int e = tid; e < kTB * kTB; e += kNT) out[e] = Y[e / kTB][e % kTB];
+}
+
+}  // namespace tc
+
+template <typename T, int CS>
+size_t trsv_cluster_smem() {
+  const size_t a = sizeof(tc::SmemSolver<T, CS>), b = sizeof(tc::SmemStream<T>);
+  size_t s = a > b ? a : b;
+  // more than half an SM's shared memory, so a solver CTA never shares its
+  // SM (and FP64 pipe) with a streaming CTA
+  return s > size_t(116) * 1024 ? s : size_t(116) * 1024;
+}
+
+template <typename T, int CS>
+static int max_clusters(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr) {
+  auto kern = tc::trsv_cluster_kernel<T, CS>;
+  const size_t smem = trsv_cluster_smem<T, CS>();
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (CS > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  attr[0].val.clusterDim.x = CS;
+  cfg.dynamicSmemBytes = smem;
+  cfg.gridDim = dim3(CS * 32);
+  int m = 0;
+  if (cudaOccupancyMaxActiveClusters(&m, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return m;
+}
+
+// Returns false when the device cannot co-schedule the clusters this needs
+// (the caller then uses the single-kernel path in trsv.cu).
+template <typename T>
+bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x) {
+  using namespace tc;
+  Context &c = ctx();
+  const int nb = int(ceil_div(n, kTB));
+  const int nch = nch_row(nb - 1) > 0 ? nch_row(nb - 1) : 1;
+  // cluster size: 16 where two or more such clusters fit, else 8 (cached per device)
+  static int cs_cache[64] = {0};
+  static int mc_cache[64] = {0};
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 8;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(kNT);
+  cfg.stream = c.stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const int dev = c.device < 64 ? c.device : 63;
+  if (cs_cache[dev] == 0) {
+    const int m16 = max_clusters<T, 16>(cfg, attr);
+    const int m8 = max_clusters<T, 8>(cfg, attr);
+    if (m16 >= 4) {
+      cs_cache[dev] = 16;
+      mc_cache[dev] = m16;
+    } else {
+      cs_cache[dev] = 8;
+      mc_cache[dev] = m8;
+    }
+  }
+  const int CS = cs_cache[dev];
+  const long maxc = mc_cache[dev];
+  if (maxc < 1) return false;
+  const long items = items_before(nb);
+  long clusters = 1 + ceil_div(items, CS);
+  if (clusters > maxc) clusters = maxc;
+  if (items > 0 && clusters < 2) return false;  // the solver needs streamers
+  attr[0].val.clusterDim.x = CS;
+  cfg.dynamicSmemBytes = CS == 16 ? trsv_cluster_smem<T, 16>() : trsv_cluster_smem<T, 8>();
+  cfg.gridDim = dim3(unsigned(clusters * CS));
+
+  // scratch: inverses, slots, flags, control words
+  const size_t inv_b = (size_t(nb) * kTB * kTB * sizeof(T) + 255) & ~size_t(255);
+  const size_t slot_b = (size_t(nb) * nch * kTB * sizeof(T) + 255) & ~size_t(255);
+  const size_t flag_b = (size_t(nb) * (1 + nch) + 2) * 4;
+  char *base = static_cast<char *>(scratch(inv_b + slot_b + flag_b));
+  Args<T> a;
+  a.n = n;
+  a.A = A;
+  a.lda = lda;
+  a.z = x;
+  a.inv = reinterpret_cast<T *>(base);
+  a.slots = reinterpret_cast<T *>(base + inv_b);
+  a.xflag = reinterpret_cast<int *>(base + inv_b + slot_b);
+  a.sflag = a.xflag + nb;
+  a.ctl = a.sflag + size_t(nb) * nch;
+  a.status = device_status_word();
+  a.nb = nb;
+  a.nch = nch;
+  a.rev = upper != trans;
+  a.trans = trans;
+  a.unit = unit;
+  EXB_CUDA(cudaMemsetAsync(a.xflag, 0, flag_b, c.stream));
+  trsv_inverse_kernel<T><<<nb, kNT, 0, c.stream>>>(a);
+  EXB_LAUNCH("trsv inverse kernel");
+  if (CS == 16)
+    EXB_CUDA(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T, 16>, a));
+  else
+    EXB_CUDA(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T, 8>, a));
+  count_launch(2);
+  c.status_pending = true;
+  return true;
+}
+
+template bool trsv_cluster<float>(bool, bool, bool, long, const float *, long, float *);
+template bool trsv_cluster<double>(bool, bool, bool, long, const double *, long, double *);
+
+}  // namespace l2
+}  // namespace exb

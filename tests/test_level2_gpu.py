@@ -109,3 +109,17 @@ def test_dtrsv_full_size_dd(cuda):
     oracle.call("dd_trsv", 122, 0, 131, n, A, n, xr, lo)
     fwd = np.abs(x - xr) / np.maximum(np.abs(xr), 1e-300)
     assert fwd.max() <= 64 * n * EPS["d"], fwd.max()
+
+
+CLUSTER = [c for p in "sd" for c in trsv_cases(p, Ns=(1000, 2049, 4160)) if c.args[8] == 1 and c.args[6] == c.args[4]]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CLUSTER, ids=lambda c: f"{c.op}-{c.label}")
+def test_trsv_clustered_sizes(cuda, case):
+    """Sizes that take the clustered solver (unit stride, n >= 192), all
+    Uplo x Trans x Diag combinations, with the residual bound."""
+    r, a = run_gpu(case)
+    o_r, o_a = run_oracle(case)
+    assert_rel1pct(a[7], o_a[7], f"{case}")
+    trsv_residual_ok(case, a[7])
