@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", choices=["bandwidth", "precision"], default="bandwidth",
+                    help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set")
+    ap.add_argument("--size", type=int, default=8192, help="M = N = K of the precision set")
     return ap.parse_args()
 
 
@@ -292,6 +295,8 @@ def main():
         if rank != 0:
             return 0
         return run_reference(args)
+    if args.workload == "precision":
+        return run_precision(args)
 
     import torch
 
@@ -437,6 +442,104 @@ def main():
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
+    return 0
+
+
+# ------------------------------------------------------ precision workload --
+def run_precision(args):
+    """Level-3 precision set (sgemm NN / ssymm Left-Upper / ssyrk Lower-NoTrans
+    at size^3 fp32, split-BF16 on tcgen05 vs plain FP32 FFMA; dgemm NN fp64
+    native), uniform[-1,1) and the stress set (sign * U[1,2) * 2^e, e in
+    [-16, 16]).  Reports TFLOP/s (device time, CUDA events) and the max and
+    median componentwise relative error against an FP64 product computed on
+    the GPU (torch float64 matmul)."""
+    import torch
+
+    import exoblas_gb300 as eb
+    from exoblas_gb300 import _native
+
+    L = _native.lib()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    eb.set_stream(stream)
+    eb.set_blocking(False)
+    n = args.size
+    vp = C.c_void_p
+    out = {}
+
+    def draw(seed, stress, dtype=torch.float32):
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        if not stress:
+            return (torch.rand(n, n, device="cuda", generator=g, dtype=torch.float64) * 2 - 1).to(dtype)
+        sign = torch.where(torch.rand(n, n, device="cuda", generator=g) < 0.5, -1.0, 1.0).double()
+        mant = 1 + torch.rand(n, n, device="cuda", generator=g, dtype=torch.float64)
+        e = torch.randint(-16, 17, (n, n), device="cuda", generator=g).double()
+        return (sign * mant * torch.exp2(e)).to(dtype)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if L.exoblas_synchronize() != 0:
+            raise RuntimeError("library failure in the precision workload")
+        return e0.elapsed_time(e1) / reps
+
+    def errs(Cg, ref, mag):
+        rel = ((Cg.double() - ref).abs() / mag.clamp_min(1e-300)).flatten()
+        return {"max": float(rel.max()), "median": float(rel.median())}
+
+    flops = {"sgemm": 2.0 * n ** 3, "ssymm": 2.0 * n ** 3, "ssyrk": float(n) * (n + 1) * n, "dgemm": 2.0 * n ** 3}
+    for stress in (False, True):
+        tag = "stress" if stress else "uniform"
+        A, B = draw(1 if stress else 0, stress), draw(11 if stress else 10, stress)
+        A64, B64 = A.double(), B.double()
+        ref_gemm = A64 @ B64
+        mag_gemm = A64.abs() @ B64.abs()
+        for mode, mname in ((eb.PRECISION_NATIVE, "ffma"), (eb.PRECISION_SPLIT_BF16, "split_bf16")):
+            eb.set_precision(mode)
+            Cg = torch.zeros(n, n, device="cuda")
+            f = lambda: L.exo_sgemm(101, 111, 111, n, n, n, 1.0, vp(A.data_ptr()), n, vp(B.data_ptr()), n, 0.0,
+                                    vp(Cg.data_ptr()), n)
+            ms = timed(f, 3 if mode == eb.PRECISION_NATIVE else 5)
+            out[f"sgemm_{mname}_{tag}"] = {"ms": round(ms, 3), "tflops": round(flops["sgemm"] / ms / 1e9, 1),
+                                          **errs(Cg, ref_gemm, mag_gemm)}
+            if not stress:
+                # ssymm Left Upper (sym(A) from A's upper triangle) and ssyrk Lower NoTrans
+                As = torch.triu(A64) + torch.triu(A64, 1).t()
+                Cs = torch.zeros(n, n, device="cuda")
+                fs = lambda: L.exo_ssymm(101, 141, 121, n, n, 1.0, vp(A.data_ptr()), n, vp(B.data_ptr()), n, 0.0,
+                                         vp(Cs.data_ptr()), n)
+                ms = timed(fs, 3 if mode == eb.PRECISION_NATIVE else 5)
+                out[f"ssymm_{mname}"] = {"ms": round(ms, 3), "tflops": round(flops["ssymm"] / ms / 1e9, 1),
+                                         **errs(Cs, As @ B64, As.abs() @ B64.abs())}
+                Ck = torch.zeros(n, n, device="cuda")
+                fk = lambda: L.exo_ssyrk(101, 122, 111, n, n, 1.0, vp(A.data_ptr()), n, 0.0, vp(Ck.data_ptr()), n)
+                ms = timed(fk, 3 if mode == eb.PRECISION_NATIVE else 5)
+                lo = torch.tril(torch.ones(n, n, device="cuda", dtype=torch.bool))
+                rk, mk = A64 @ A64.t(), A64.abs() @ A64.abs().t()
+                out[f"ssyrk_{mname}"] = {"ms": round(ms, 3), "tflops": round(flops["ssyrk"] / ms / 1e9, 1),
+                                         **errs(Ck[lo], rk[lo], mk[lo])}
+        eb.set_precision(eb.PRECISION_NATIVE)
+        del ref_gemm, mag_gemm
+    # dgemm native (FP64 DFMA); Ozaki emulation reported when available
+    Ad, Bd = draw(20, False, torch.float64), draw(21, False, torch.float64)
+    Cd = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+    fd = lambda: L.exo_dgemm(101, 111, 111, n, n, n, 1.0, vp(Ad.data_ptr()), n, vp(Bd.data_ptr()), n, 0.0,
+                             vp(Cd.data_ptr()), n)
+    ms = timed(fd, 1)
+    out["dgemm_native"] = {"ms": round(ms, 3), "tflops": round(flops["dgemm"] / ms / 1e9, 2)}
+    line = {
+        "metric": METRIC, "unit": "TFLOP/s", "workload": f"level-3 precision set {n}^3",
+        "value": out.get("sgemm_split_bf16_uniform", {}).get("tflops"),
+        "speedup_split_over_ffma": round(out["sgemm_split_bf16_uniform"]["tflops"] / out["sgemm_ffma_uniform"]["tflops"], 2),
+        "results": out,
+    }
+    print(json.dumps(line))
     return 0
 
 

@@ -33,10 +33,40 @@ static void inc_ok(long inc, const char *what) {
 }
 
 // Level-3 dispatch on the thread's precision mode.
-template <typename T>
-static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb,
-                          T beta, T *C, long ldc) {
-  l3::gemm_simt<T>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+static bool split_mode() { return ctx().precision == EXOBLAS_PRECISION_SPLIT_BF16; }
+
+static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, float alpha, const float *A, long lda,
+                          const float *B, long ldb, float beta, float *C, long ldc) {
+  if (split_mode() && k > 0)
+    l3::gemm_split_bf16(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  else
+    l3::gemm_simt<float>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda,
+                          const double *B, long ldb, double beta, double *C, long ldc) {
+  l3::gemm_simt<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+static void symm_dispatch(bool left, bool upper, long m, long n, float alpha, const float *A, long lda, const float *B,
+                          long ldb, float beta, float *C, long ldc) {
+  if (split_mode())
+    l3::symm_split_bf16(left, upper, m, n, alpha, A, lda, B, ldb, beta, C, ldc);
+  else
+    l3::symm_simt<float>(left, upper, m, n, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+static void symm_dispatch(bool left, bool upper, long m, long n, double alpha, const double *A, long lda,
+                          const double *B, long ldb, double beta, double *C, long ldc) {
+  l3::symm_simt<double>(left, upper, m, n, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+static void syrk_dispatch(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
+                          float *C, long ldc) {
+  if (split_mode() && k > 0)
+    l3::syrk_split_bf16(upper, trans, n, k, alpha, A, lda, beta, C, ldc);
+  else
+    l3::syrk_simt<float>(upper, trans, n, k, alpha, A, lda, beta, C, ldc);
+}
+static void syrk_dispatch(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, double beta,
+                          double *C, long ldc) {
+  l3::syrk_simt<double>(upper, trans, n, k, alpha, A, lda, beta, C, ldc);
 }
 
 // ------------------------------------------------------------------ level 2
@@ -199,7 +229,7 @@ static void gemm_entry(const char *fn, int Order, int TransA, int TransB, int M,
     const T *dA = K > 0 ? st.mat(A, ar, ac, lda, false) : A;
     const T *dB = K > 0 ? st.mat(B, br, bc, ldb, false) : B;
     T *dC = st.mat(C, M, N, ldc, true);
-    gemm_dispatch<T>(ta, tb, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc);
+    gemm_dispatch(ta, tb, M, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc);
     st.finish();
   });
 }
@@ -222,7 +252,7 @@ static void symm_entry(const char *fn, int Order, int Side, int Uplo, int M, int
     const T *dA = st.mat(A, ka, ka, lda, false);
     const T *dB = st.mat(B, M, N, ldb, false);
     T *dC = st.mat(C, M, N, ldc, true);
-    l3::symm_simt<T>(left, Uplo == kUpper, M, N, alpha, dA, lda, dB, ldb, beta, dC, ldc);
+    symm_dispatch(left, Uplo == kUpper, M, N, alpha, dA, lda, dB, ldb, beta, dC, ldc);
     st.finish();
   });
 }
@@ -243,7 +273,7 @@ static void syrk_entry(const char *fn, int Order, int Uplo, int Trans, int N, in
     Stager st;
     const T *dA = K > 0 ? st.mat(A, ar, ac, lda, false) : A;
     T *dC = st.mat(C, N, N, ldc, true);
-    l3::syrk_simt<T>(Uplo == kUpper, trans, N, K, alpha, dA, lda, beta, dC, ldc);
+    syrk_dispatch(Uplo == kUpper, trans, N, K, alpha, dA, lda, beta, dC, ldc);
     st.finish();
   });
 }

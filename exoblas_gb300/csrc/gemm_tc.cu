@@ -1,0 +1,577 @@
+// Level 3 on the 5th-generation tensor cores (tcgen05, sm_103a): FP32
+// sgemm / ssymm / ssyrk through a split-BF16 representation.
+//
+// Each FP32 operand x is split into three BF16 terms x = x0 + x1 + x2
+// (x0 = bf16(x), x1 = bf16(x - x0), x2 = bf16(x - x0 - x1)), 24 significand
+// bits in all.  C = alpha * op(A) op(B) + beta * C is formed from the six
+// products whose weight is at least 2^-16 relative to the leading one,
+// issued from small to large:
+//   lo += a2 b0 + a1 b1 + a0 b2 + a1 b0 + a0 b1,   hi += a0 b0,
+// both accumulated in FP32 in tensor memory.  Every bf16 x bf16 product is
+// exact in FP32; keeping the leading term in its own accumulator keeps the
+// small corrections from being absorbed by it.  The tensor core's FP32
+// accumulation does not round to nearest at every step, so K is cut into
+// chunks of kChunk: each chunk is accumulated in tensor memory (two buffers,
+// alternating), and the epilogue warps fold every finished chunk into
+// per-element FP32 sums carried with a TwoSum compensation term, then form
+// alpha * sum + beta * C once at the end of the tile.
+//
+// Kernel structure (one CTA per SM, persistent over 128 x 128 output tiles):
+//   warp 0       TMA producer: per k-block, the 3 slices of A and of B (six
+//                16 KiB 128-byte-swizzled tiles, one 96 KiB stage, 2 stages)
+//   warp 1       allocates tensor memory; one thread issues tcgen05.mma
+//                (M = 128, N = 128, K = 16) and tcgen05.commit
+//   warps 2..17  epilogue: per chunk, tcgen05.ld of both accumulators of a
+//                buffer (four warps per 32-lane quarter, 32 columns each);
+//                per tile, beta * C fused into the store (syrk: elements
+//                outside the triangle are left alone)
+// Synchronisation is by mbarriers; every wait is bounded by a clock budget
+// after which the CTA records a timeout in the device status word, drains
+// what it started and frees its tensor memory.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "runtime.h"
+
+namespace exb {
+namespace l3 {
+namespace t5 {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int kSlices = 3;
+constexpr int kStages = 2;
+constexpr int kTileBytes = BM * BK * 2;  // 16 KiB (BN == BM)
+constexpr int kStageBytes = 2 * kSlices * kTileBytes;
+constexpr int kEpiWarps = 16;
+constexpr int kEpiCols = BN / (kEpiWarps / 4);  // columns per epilogue warp
+constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr int kChunkKB = 4;      // k-blocks per accumulation chunk (K = 256)
+constexpr int kTmemCols = 512;   // two buffers x (hi at column 0, lo at BN)
+constexpr long long kTimeoutCycles = 4ll << 30;  // ~2 s at 2 GHz
+
+// products in issue order (small to large); acc 1 = lo, 0 = hi
+__constant__ signed char kProdA[6] = {2, 1, 0, 1, 0, 0};
+__constant__ signed char kProdB[6] = {0, 1, 2, 0, 1, 0};
+__constant__ signed char kProdAcc[6] = {1, 1, 1, 1, 1, 0};
+
+struct Params {
+  int M, N, K;
+  int Mp, Np;  // slice row pitch (multiples of 128)
+  int kblocks;
+  int mtiles, ntiles, tiles;
+  int tri;  // 0 full, 1 lower, 2 upper (syrk)
+  float alpha, beta;
+  float *C;
+  long ldc;
+  int *status;
+};
+
+// ------------------------------------------------------------ PTX helpers --
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false on timeout or when another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *status) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (*abort_flag) return false;
+    if (clock64() - t0 > kTimeoutCycles) {
+      *abort_flag = 1;
+      atomicExch(status, 1);
+      return false;
+    }
+  }
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+// Shared-memory matrix descriptor: K-major operand tile of 8-row x 128-byte
+// swizzle atoms (128B swizzle), atoms 1024 bytes apart along M/N.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= uint64_t((saddr & 0x3FFFF) >> 4);  // start address
+  d |= uint64_t(1) << 16;                 // leading byte offset (unused with 128B swizzle)
+  d |= uint64_t(1024 >> 4) << 32;         // stride byte offset: next 8-row group
+  d |= uint64_t(1) << 46;                 // descriptor version
+  d |= uint64_t(2) << 61;                 // 128-byte swizzle
+  return d;
+}
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+// 32 consecutive TMEM columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 16 consecutive TMEM columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 8 consecutive TMEM columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// tile index -> (mt, nt); grouped raster of 8 m-tiles for L2 reuse; triangle
+// tiles for syrk (lower: nt <= mt, upper: nt >= mt)
+__device__ __forceinline__ void tile_coords(const Params &p, int t, int &mt, int &nt) {
+  if (p.tri) {
+    int r = int((sqrtf(8.f * float(t) + 1.f) - 1.f) * 0.5f);
+    while (r * (r + 1) / 2 > t) --r;
+    while ((r + 1) * (r + 2) / 2 <= t) ++r;
+    const int c = t - r * (r + 1) / 2;
+    mt = p.tri == 1 ? r : c;
+    nt = p.tri == 1 ? c : r;
+    return;
+  }
+  constexpr int G = 8;
+  const int group = t / (G * p.ntiles);
+  const int first = group * G;
+  const int gm = p.mtiles - first < G ? p.mtiles - first : G;
+  const int in = t - group * G * p.ntiles;
+  mt = first + in % gm;
+  nt = in / gm;
+}
+
+// ---------------------------------------------------------------- kernel --
+__global__ void __launch_bounds__(kThreads, 1)
+    split_bf16_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                           Params p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned stage area (128B-swizzle atoms need it)
+  unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accfull[2], accempty[2], drain;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_flag;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], kEpiWarps);  // one arrival per epilogue warp
+    }
+    mbar_init(&drain, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(&tmem_slot, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------ TMA producer --
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+      int stage = 0;
+      uint32_t round = 0;
+      long issued = 0;
+      for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
+        int mt, nt;
+        tile_coords(p, t, mt, nt);
+        for (int kb = 0; kb < p.kblocks; ++kb) {
+          if (!mbar_wait(&empty[stage], (round & 1) ^ 1, &abort_flag, p.status)) break;
+          mbar_expect_tx(&full[stage], kStageBytes);
+          unsigned char *st = smem + stage * kStageBytes;
+#pragma unroll
+          for (int s = 0; s < kSlices; ++s) {
+            tma_load_2d(st + s * kTileBytes, &mapA, &full[stage], kb * BK, s * p.Mp + mt * BM);
+            tma_load_2d(st + (kSlices + s) * kTileBytes, &mapB, &full[stage], kb * BK, s * p.Np + nt * BN);
+          }
+          ++issued;
+          if (++stage == kStages) {
+            stage = 0;
+            ++round;
+          }
+        }
+      }
+      // drain: every issued stage's copies must land before the CTA exits
+      for (int s = 0; s < kStages && issued > 0; ++s) {
+        // the most recent use of each stage is round r_s; wait for its fill
+        long uses = issued / kStages + (s < issued % kStages ? 1 : 0);
+        if (uses == 0) continue;
+        const uint32_t par = uint32_t((uses - 1) & 1);
+        const long long t0 = clock64();
+        while (!mbar_try_wait(&full[s], par) && clock64() - t0 < kTimeoutCycles) {
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------- MMA issuer --
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t round = 0;
+      uint32_t chunk = 0;  // global chunk counter: buffer chunk & 1
+      bool any = false;
+      for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
+        for (int kb0 = 0; kb0 < p.kblocks && !abort_flag; kb0 += kChunkKB) {
+          const int buf = int(chunk & 1);
+          if (!mbar_wait(&accempty[buf], ((chunk >> 1) & 1) ^ 1, &abort_flag, p.status)) break;
+          tc_fence_after();
+          const uint32_t accbase = tmem + uint32_t(buf * 2 * BN);
+          const int kb1 = kb0 + kChunkKB < p.kblocks ? kb0 + kChunkKB : p.kblocks;
+          for (int kb = kb0; kb < kb1; ++kb) {
+            if (!mbar_wait(&full[stage], round & 1, &abort_flag, p.status)) break;
+            tc_fence_after();
+            const uint32_t sbase = smem_u32(smem + stage * kStageBytes);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+              const uint32_t acc = accbase + (kProdAcc[q] ? BN : 0);
+              const uint64_t da = sdesc_sw128(sbase + kProdA[q] * kTileBytes);
+              const uint64_t db = sdesc_sw128(sbase + (kSlices + kProdB[q]) * kTileBytes);
+              // the first product into each accumulator of a chunk overwrites it
+              const bool first = kb == kb0 && (q == 0 || q == 5);
+#pragma unroll
+              for (int k16 = 0; k16 < BK / 16; ++k16)
+                umma(acc, da + uint64_t(2 * k16), db + uint64_t(2 * k16), (first && k16 == 0) ? 0u : 1u);
+            }
+            umma_commit(&empty[stage]);  // frees the stage when these MMAs finish
+            any = true;
+            if (++stage == kStages) {
+              stage = 0;
+              ++round;
+            }
+          }
+          if (abort_flag) break;
+          umma_commit(&accfull[buf]);
+          ++chunk;
+        }
+      }
+      // drain outstanding MMAs before tensor memory is released
+      if (any) {
+        umma_commit(&drain);
+        const long long t0 = clock64();
+        while (!mbar_try_wait(&drain, 0) && clock64() - t0 < kTimeoutCycles) {
+        }
+      }
+    }
+  } else {
+    // --------------------------------------------------------- epilogue --
+    const int q = warp & 3;                 // tensor-memory lane quarter this warp may read
+    const int part = (warp - 2) >> 2;       // columns [kEpiCols part, kEpiCols (part + 1))
+    const int row = q * 32 + lane;
+    uint32_t chunk = 0;
+    for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
+      int mt, nt;
+      tile_coords(p, t, mt, nt);
+      float sum[kEpiCols], comp[kEpiCols];
+#pragma unroll
+      for (int j = 0; j < kEpiCols; ++j) sum[j] = comp[j] = 0.f;
+      bool ok = true;
+      for (int kb0 = 0; kb0 < p.kblocks; kb0 += kChunkKB) {
+        const int buf = int(chunk & 1);
+        if (!mbar_wait(&accfull[buf], (chunk >> 1) & 1, &abort_flag, p.status)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t tb = tmem + (uint32_t(q * 32) << 16) + uint32_t(buf * 2 * BN + part * kEpiCols);
+#pragma unroll
+        for (int c = 0; c < kEpiCols; c += 8) {
+          float hi[8], lo[8];
+          tmem_ld8(tb + c, hi);
+          tmem_ld8(tb + BN + c, lo);
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            // TwoSum of the running sum and this chunk's value
+            const float v = hi[j] + lo[j];
+            const float s1 = sum[c + j] + v;
+            const float z = s1 - sum[c + j];
+            comp[c + j] += (sum[c + j] - (s1 - z)) + (v - z);
+            sum[c + j] = s1;
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&accempty[buf]);
+        ++chunk;
+      }
+      if (!ok) break;
+      const long gi = long(mt) * BM + row;
+      if (gi < p.M) {
+        float *crow = p.C + gi * p.ldc;
+        const long gj0 = long(nt) * BN + part * kEpiCols;
+#pragma unroll
+        for (int j = 0; j < kEpiCols; ++j) {
+          const long gj = gj0 + j;
+          const bool in = gj < p.N && !(p.tri == 1 && gj > gi) && !(p.tri == 2 && gj < gi);
+          if (in) crow[gj] = p.alpha * (sum[j] + comp[j]) + p.beta * crow[gj];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+// --------------------------------------------------------------- split ----
+// out[s][r][k] (s < 3, r < Rp, k < Kp, bf16) for the logical rows x K operand
+// X(r, k); zero outside rows x K.  32 x 32 tiles through shared memory so
+// both the source (either orientation) and the K-major output are coalesced.
+template <class Op>
+__global__ void split3_kernel(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out) {
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  const bool src_k_fast = X.k_contiguous();
+  for (int i = ty; i < 32; i += 8) {
+    // source read: consecutive threads along the source's contiguous index
+    const int r = src_k_fast ? r0 + i : r0 + tx;
+    const int k = src_k_fast ? k0 + tx : k0 + i;
+    float v = (r < rows && k < K) ? X(r, k) : 0.f;
+    if (src_k_fast)
+      tile[i][tx] = v;
+    else
+      tile[tx][i] = v;
+  }
+  __syncthreads();
+  const size_t slice = size_t(Rp) * Kp;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i, k = k0 + tx;
+    if (r >= Rp || k >= Kp) continue;
+    const float v = tile[i][tx];
+    const __nv_bfloat16 b0 = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(b0);
+    const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+    const float r2 = r1 - __bfloat162float(b1);
+    const __nv_bfloat16 b2 = __float2bfloat16_rn(r2);
+    const size_t o = size_t(r) * Kp + k;
+    out[o] = b0;
+    out[slice + o] = b1;
+    out[2 * slice + o] = b2;
+  }
+}
+
+// operand views: X(r, k) for the logical rows x K operand
+struct ViewPlain {
+  const float *p;
+  long ld;
+  bool t;  // element (r, k) at p[k * ld + r]
+  __device__ float operator()(int r, int k) const { return t ? p[long(k) * ld + r] : p[long(r) * ld + k]; }
+  __device__ bool k_contiguous() const { return !t; }
+};
+struct ViewSym {
+  const float *p;
+  long ld;
+  bool upper;
+  __device__ float operator()(int r, int k) const {
+    const bool stored = upper ? (k >= r) : (k <= r);
+    return stored ? p[long(r) * ld + k] : p[long(k) * ld + r];
+  }
+  __device__ bool k_contiguous() const { return true; }
+};
+
+// ---------------------------------------------------------------- host ----
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(f);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// 2-D bf16 tensor map over `rows` x Kp (Kp contiguous), box 64 x 128, 128B swizzle
+static CUtensorMap make_map(const void *base, long rows, long Kp) {
+  CUtensorMap m;
+  EncodeTiled enc = encode_fn();
+  if (!enc) fail(EXOBLAS_NOT_SUPPORTED, "cuTensorMapEncodeTiled is unavailable");
+  const cuuint64_t dims[2] = {cuuint64_t(Kp), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(Kp) * 2};
+  const cuuint32_t box[2] = {BK, BM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(EXOBLAS_CUDA_ERROR, "cuTensorMapEncodeTiled failed");
+  return m;
+}
+
+template <class Op>
+static void split(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out) {
+  dim3 grid(unsigned(ceil_div(Kp, 32)), unsigned(ceil_div(Rp, 32)));
+  split3_kernel<Op><<<grid, 256, 0, ctx().stream>>>(X, rows, K, Rp, Kp, out);
+  EXB_LAUNCH("bf16 split kernel");
+  count_launch();
+}
+
+static int round_up(long v, int m) { return int((v + m - 1) / m * m); }
+
+// C (M x N) = alpha * X_A X_B^T + beta * C where X_A is M x K and X_B is
+// N x K (both logical, row r / column k).  tri: syrk triangle; same_ab:
+// X_B is X_A (syrk), split once.
+template <class OA, class OB>
+static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, float *C, long ldc, int tri, bool same_ab) {
+  Context &c = ctx();
+  const int Kp = round_up(K, BK), Mp = round_up(M, BM), Np = round_up(N, BN);
+  const size_t a_elems = size_t(kSlices) * Mp * Kp, b_elems = same_ab ? 0 : size_t(kSlices) * Np * Kp;
+  char *ws = static_cast<char *>(scratch((a_elems + b_elems) * 2 + 256));
+  __nv_bfloat16 *sa = reinterpret_cast<__nv_bfloat16 *>(ws);
+  __nv_bfloat16 *sb = same_ab ? sa : sa + a_elems;
+  split(xa, M, K, Mp, Kp, sa);
+  if (!same_ab) split(xb, N, K, Np, Kp, sb);
+  const CUtensorMap ma = make_map(sa, long(kSlices) * Mp, Kp);
+  const CUtensorMap mb = make_map(sb, long(kSlices) * (same_ab ? Mp : Np), Kp);
+  Params p;
+  p.M = M;
+  p.N = N;
+  p.K = K;
+  p.Mp = Mp;
+  p.Np = same_ab ? Mp : Np;
+  p.kblocks = Kp / BK;
+  p.mtiles = Mp / BM;
+  p.ntiles = Np / BN;
+  p.tri = tri;
+  p.tiles = tri ? p.mtiles * (p.mtiles + 1) / 2 : p.mtiles * p.ntiles;
+  p.alpha = alpha;
+  p.beta = beta;
+  p.C = C;
+  p.ldc = ldc;
+  p.status = device_status_word();
+  static bool attr = false;
+  const int smem = kStages * kStageBytes + 1024;
+  if (!attr) {
+    EXB_CUDA(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  const int grid = p.tiles < c.sm_count ? p.tiles : c.sm_count;
+  split_bf16_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(ma, mb, p);
+  EXB_LAUNCH("split-bf16 tcgen05 gemm kernel");
+  count_launch();
+  c.status_pending = true;
+}
+
+}  // namespace t5
+
+void gemm_split_bf16(bool ta, bool tb, long m, long n, long k, float alpha, const float *A, long lda, const float *B,
+                     long ldb, float beta, float *C, long ldc) {
+  if (m <= 0 || n <= 0) return;
+  // op(B) is k x n; its K-major form is row j, column kk = op(B)[kk][j]
+  t5::run(t5::ViewPlain{A, lda, ta}, t5::ViewPlain{B, ldb, !tb}, int(m), int(n), int(k), alpha, beta, C, ldc, 0,
+          false);
+}
+
+void symm_split_bf16(bool left, bool upper, long m, long n, float alpha, const float *A, long lda, const float *B,
+                     long ldb, float beta, float *C, long ldc) {
+  if (m <= 0 || n <= 0) return;
+  if (left)  // C = sym(A) B: X_A = sym(A) (m x m), X_B(j, kk) = B[kk][j]
+    t5::run(t5::ViewSym{A, lda, upper}, t5::ViewPlain{B, ldb, true}, int(m), int(n), int(m), alpha, beta, C, ldc, 0,
+            false);
+  else  // C = B sym(A): X_A = B (m x n), X_B = sym(A) (n x n, symmetric)
+    t5::run(t5::ViewPlain{B, ldb, false}, t5::ViewSym{A, lda, upper}, int(m), int(n), int(n), alpha, beta, C, ldc, 0,
+            false);
+}
+
+void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
+                     float *C, long ldc) {
+  if (n <= 0) return;
+  // X_A = op(A) (n x k): NoTrans row i of A, Trans column i of A
+  t5::ViewPlain x{A, lda, trans};
+  t5::run(x, x, int(n), int(n), int(k), alpha, beta, C, ldc, upper ? 2 : 1, true);
+}
+
+}  // namespace l3
+}  // namespace exb

@@ -60,6 +60,13 @@ void symm_simt(bool left, bool upper, long m, long n, T alpha, const T *A, long 
                T *C, long ldc);
 template <typename T>
 void syrk_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, T beta, T *C, long ldc);
+// tcgen05 tensor-core paths: FP32 through three BF16 terms per operand
+void gemm_split_bf16(bool ta, bool tb, long m, long n, long k, float alpha, const float *A, long lda, const float *B,
+                     long ldb, float beta, float *C, long ldc);
+void symm_split_bf16(bool left, bool upper, long m, long n, float alpha, const float *A, long lda, const float *B,
+                     long ldb, float beta, float *C, long ldc);
+void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
+                     float *C, long ldc);
 }  // namespace l3
 
 }  // namespace exb
