@@ -526,17 +526,41 @@ def run_precision(args):
                                          **errs(Ck[lo], rk[lo], mk[lo])}
         eb.set_precision(eb.PRECISION_NATIVE)
         del ref_gemm, mag_gemm
-    # dgemm native (FP64 DFMA); Ozaki emulation reported when available
-    Ad, Bd = draw(20, False, torch.float64), draw(21, False, torch.float64)
-    Cd = torch.zeros(n, n, device="cuda", dtype=torch.float64)
-    fd = lambda: L.exo_dgemm(101, 111, 111, n, n, n, 1.0, vp(Ad.data_ptr()), n, vp(Bd.data_ptr()), n, 0.0,
-                             vp(Cd.data_ptr()), n)
-    ms = timed(fd, 1)
-    out["dgemm_native"] = {"ms": round(ms, 3), "tflops": round(flops["dgemm"] / ms / 1e9, 2)}
+    # dgemm: native FP64 DFMA vs Ozaki slice emulation; error on 256 sampled
+    # entries against the double-double oracle (CPU)
+    import numpy as np
+
+    import oracle
+
+    for stress in (False, True):
+        tag = "stress" if stress else "uniform"
+        Ad, Bd = draw(20 if not stress else 22, stress, torch.float64), draw(21 if not stress else 23, stress,
+                                                                             torch.float64)
+        Ah, Bh = Ad.cpu().numpy(), Bd.cpu().numpy()
+        g = np.random.default_rng(9)
+        rows = g.integers(0, n, 256).astype(np.int64)
+        cols = g.integers(0, n, 256).astype(np.int64)
+        ref = np.zeros(256)
+        oracle.call("dd_gemm_entries", 0, 0, n, 1.0, Ah, n, Bh, n, 0.0, None, n, rows, cols, 256, ref)
+        mag = np.einsum("ik,ki->i", np.abs(Ah[rows]), np.abs(Bh[:, cols]))
+        for mode, mname in ((eb.PRECISION_NATIVE, "native"), (eb.PRECISION_OZAKI, "ozaki")):
+            if mode == eb.PRECISION_NATIVE and stress:
+                continue
+            eb.set_precision(mode)
+            Cd = torch.zeros(n, n, device="cuda", dtype=torch.float64)
+            fd = lambda: L.exo_dgemm(101, 111, 111, n, n, n, 1.0, vp(Ad.data_ptr()), n, vp(Bd.data_ptr()), n, 0.0,
+                                     vp(Cd.data_ptr()), n)
+            ms = timed(fd, 1 if mode == eb.PRECISION_NATIVE else 3)
+            got = Cd.cpu().numpy()[rows, cols]
+            rel = np.abs(got - ref) / mag
+            out[f"dgemm_{mname}_{tag}"] = {"ms": round(ms, 3), "tflops": round(flops["dgemm"] / ms / 1e9, 2),
+                                           "max": float(rel.max()), "median": float(np.median(rel))}
+        eb.set_precision(eb.PRECISION_NATIVE)
     line = {
         "metric": METRIC, "unit": "TFLOP/s", "workload": f"level-3 precision set {n}^3",
         "value": out.get("sgemm_split_bf16_uniform", {}).get("tflops"),
         "speedup_split_over_ffma": round(out["sgemm_split_bf16_uniform"]["tflops"] / out["sgemm_ffma_uniform"]["tflops"], 2),
+        "speedup_ozaki_over_dfma": round(out["dgemm_ozaki_uniform"]["tflops"] / out["dgemm_native_uniform"]["tflops"], 2),
         "results": out,
     }
     print(json.dumps(line))

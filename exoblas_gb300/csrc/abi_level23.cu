@@ -44,6 +44,9 @@ static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, float alpha,
 }
 static void gemm_dispatch(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda,
                           const double *B, long ldb, double beta, double *C, long ldc) {
+  if (ctx().precision == EXOBLAS_PRECISION_OZAKI && k > 0 &&
+      l3::dgemm_ozaki(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc))
+    return;
   l3::gemm_simt<double>(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 static void symm_dispatch(bool left, bool upper, long m, long n, float alpha, const float *A, long lda, const float *B,

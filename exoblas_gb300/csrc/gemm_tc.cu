@@ -37,6 +37,7 @@
 #include "common.cuh"
 #include "kernels.h"
 #include "runtime.h"
+#include "tc5.cuh"
 
 namespace exb {
 namespace l3 {
@@ -52,7 +53,6 @@ constexpr int kEpiCols = BN / (kEpiWarps / 4);  // columns per epilogue warp
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr int kChunkKB = 4;      // k-blocks per accumulation chunk (K = 256)
 constexpr int kTmemCols = 512;   // two buffers x (hi at column 0, lo at BN)
-constexpr long long kTimeoutCycles = 4ll << 30;  // ~2 s at 2 GHz
 
 // products in issue order (small to large); acc 1 = lo, 0 = hi
 __constant__ signed char kProdA[6] = {2, 1, 0, 1, 0, 0};
@@ -71,129 +71,8 @@ struct Params {
   int *status;
 };
 
-// ------------------------------------------------------------ PTX helpers --
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait; false on timeout or when another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *status) {
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (*abort_flag) return false;
-    if (clock64() - t0 > kTimeoutCycles) {
-      *abort_flag = 1;
-      atomicExch(status, 1);
-      return false;
-    }
-  }
-  return true;
-}
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-// Shared-memory matrix descriptor: K-major operand tile of 8-row x 128-byte
-// swizzle atoms (128B swizzle), atoms 1024 bytes apart along M/N.
-__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= uint64_t((saddr & 0x3FFFF) >> 4);  // start address
-  d |= uint64_t(1) << 16;                 // leading byte offset (unused with 128B swizzle)
-  d |= uint64_t(1024 >> 4) << 32;         // stride byte offset: next 8-row group
-  d |= uint64_t(1) << 46;                 // descriptor version
-  d |= uint64_t(2) << 61;                 // 128-byte swizzle
-  return d;
-}
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
-
-__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-
-// 32 consecutive TMEM columns of this warp's 32 lanes
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 16 consecutive TMEM columns of this warp's 32 lanes
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// 8 consecutive TMEM columns of this warp's 32 lanes
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr)
-               : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
+constexpr uint32_t kIdesc = tc5::idesc_bf16_f32(BM, BN);
+using namespace tc5;
 
 // tile index -> (mt, nt); grouped raster of 8 m-tiles for L2 reuse; triangle
 // tiles for syrk (lower: nt <= mt, upper: nt >= mt)
@@ -313,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const bool first = kb == kb0 && (q == 0 || q == 5);
 #pragma unroll
               for (int k16 = 0; k16 < BK / 16; ++k16)
-                umma(acc, da + uint64_t(2 * k16), db + uint64_t(2 * k16), (first && k16 == 0) ? 0u : 1u);
+                umma(acc, da + uint64_t(2 * k16), db + uint64_t(2 * k16), kIdesc, (first && k16 == 0) ? 0u : 1u);
             }
             umma_commit(&empty[stage]);  // frees the stage when these MMAs finish
             any = true;
@@ -456,40 +335,6 @@ struct ViewSym {
 };
 
 // ---------------------------------------------------------------- host ----
-using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiled encode_fn() {
-  static EncodeTiled fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void *f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiled>(f);
-    cudaGetLastError();
-  });
-  return fn;
-}
-
-// 2-D bf16 tensor map over `rows` x Kp (Kp contiguous), box 64 x 128, 128B swizzle
-static CUtensorMap make_map(const void *base, long rows, long Kp) {
-  CUtensorMap m;
-  EncodeTiled enc = encode_fn();
-  if (!enc) fail(EXOBLAS_NOT_SUPPORTED, "cuTensorMapEncodeTiled is unavailable");
-  const cuuint64_t dims[2] = {cuuint64_t(Kp), cuuint64_t(rows)};
-  const cuuint64_t strides[1] = {cuuint64_t(Kp) * 2};
-  const cuuint32_t box[2] = {BK, BM};
-  const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) fail(EXOBLAS_CUDA_ERROR, "cuTensorMapEncodeTiled failed");
-  return m;
-}
-
 template <class Op>
 static void split(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out) {
   dim3 grid(unsigned(ceil_div(Kp, 32)), unsigned(ceil_div(Rp, 32)));
@@ -513,8 +358,8 @@ static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, floa
   __nv_bfloat16 *sb = same_ab ? sa : sa + a_elems;
   split(xa, M, K, Mp, Kp, sa);
   if (!same_ab) split(xb, N, K, Np, Kp, sb);
-  const CUtensorMap ma = make_map(sa, long(kSlices) * Mp, Kp);
-  const CUtensorMap mb = make_map(sb, long(kSlices) * (same_ab ? Mp : Np), Kp);
+  const CUtensorMap ma = make_map(sa, long(kSlices) * Mp, Kp, BK, BM);
+  const CUtensorMap mb = make_map(sb, long(kSlices) * (same_ab ? Mp : Np), Kp, BK, BN);
   Params p;
   p.M = M;
   p.N = N;
@@ -531,11 +376,12 @@ static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, floa
   p.C = C;
   p.ldc = ldc;
   p.status = device_status_word();
-  static bool attr = false;
+  static bool attr[64] = {};
   const int smem = kStages * kStageBytes + 1024;
-  if (!attr) {
+  const int dev = c.device < 64 ? c.device : 63;
+  if (!attr[dev]) {
     EXB_CUDA(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = true;
+    attr[dev] = true;
   }
   const int grid = p.tiles < c.sm_count ? p.tiles : c.sm_count;
   split_bf16_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(ma, mb, p);

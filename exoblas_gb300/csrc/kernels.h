@@ -67,6 +67,10 @@ void symm_split_bf16(bool left, bool upper, long m, long n, float alpha, const f
                      long ldb, float beta, float *C, long ldc);
 void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
                      float *C, long ldc);
+// tcgen05 Ozaki slice emulation of dgemm; false when an input is not finite
+// (nothing written; the caller uses the FP64 FMA kernel)
+bool dgemm_ozaki(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda, const double *B,
+                 long ldb, double beta, double *C, long ldc);
 }  // namespace l3
 
 }  // namespace exb
