@@ -69,7 +69,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["bandwidth", "precision"], default="bandwidth",
+    ap.add_argument("--workload", choices=["bandwidth", "precision", "batch"], default="bandwidth",
                     help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set")
     ap.add_argument("--size", type=int, default=8192, help="M = N = K of the precision set")
     return ap.parse_args()
@@ -297,6 +297,8 @@ def main():
         return run_reference(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "batch":
+        return run_batch(args)
 
     import torch
 
@@ -562,6 +564,90 @@ def run_precision(args):
         "speedup_split_over_ffma": round(out["sgemm_split_bf16_uniform"]["tflops"] / out["sgemm_ffma_uniform"]["tflops"], 2),
         "speedup_ozaki_over_dfma": round(out["dgemm_ozaki_uniform"]["tflops"] / out["dgemm_native_uniform"]["tflops"], 2),
         "results": out,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------- batch workload --
+def run_batch(args):
+    """4096 independent sgemm / dgemv / strsv instances (op uniform per
+    instance, m, n, k log-uniform in [16, 2048], seed 7) in one persistent
+    launch replayed from a CUDA graph, against the same calls issued one at a
+    time through the exo_* C ABI (device pointers, non-blocking)."""
+    import tempfile as tf
+
+    import torch
+
+    import exoblas_gb300 as eb
+    from exoblas_gb300 import _native, batch, workloads
+
+    L = _native.lib()
+    torch.cuda.set_device(0)
+    os.environ.setdefault("EXOBLAS_TUNE_CACHE", os.path.join(tf.gettempdir(), "exoblas_tune.json"))
+    t0 = time.perf_counter()
+    batch.tune()
+    tune_s = time.perf_counter() - t0
+    ops, shapes, arena, views = workloads.batch_config(torch, "cuda")
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    eb.set_stream(stream)
+    eb.set_blocking(False)
+    plan = batch.BatchPlan(ops)
+    info = plan.info()
+    for _ in range(args.warmup):
+        plan.graph_launch()
+    torch.cuda.synchronize()
+    K = max(3, min(args.steps, 20))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.25)
+    e0.record(stream)
+    for _ in range(K):
+        plan.graph_launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    batch_ms = e0.elapsed_time(e1) / K
+    # the same calls one by one through the C ABI
+    vp = C.c_void_p
+    calls = []
+    for (op, dims, t), o in zip(views, ops):
+        if op == "sgemm":
+            m, n, k = dims
+            calls.append(lambda o=o, m=m, n=n, k=k: L.exo_sgemm(101, 111, 111, m, n, k, 1.0, vp(o.A), k, vp(o.B), n,
+                                                                0.5, vp(o.C), n))
+        elif op == "dgemv":
+            m, n = dims
+            calls.append(lambda o=o, m=m, n=n: L.exo_dgemv(101, 111, m, n, 1.0, vp(o.A), n, vp(o.B), 1, 0.5, vp(o.C), 1))
+        else:
+            (n,) = dims
+            calls.append(lambda o=o, n=n: L.exo_strsv(101, 122, 111, 131, n, vp(o.A), n, vp(o.C), 1))
+    for f in calls:
+        f()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    w0 = time.perf_counter()
+    for f in calls:
+        f()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    percall_wall_ms = (time.perf_counter() - w0) * 1e3
+    percall_ms = e0.elapsed_time(e1)
+    plan.close()
+    n = len(ops)
+    counts = {k: sum(1 for s in shapes if s[0] == k) for k in workloads.OPS}
+    line = {
+        "metric": METRIC, "workload": "batch: 4096 mixed sgemm/dgemv/strsv, m,n,k log-uniform [16,2048], seed 7",
+        "unit": "solves/s", "value": round(n / (batch_ms * 1e-3), 1), "ms_per_batch": round(batch_ms, 3),
+        "units": info["units"], "counts": counts,
+        "sgemm_gflop": round(info["flops"] / 1e9, 1), "gemv_trsv_gb": round(info["bytes"] / 1e9, 2),
+        "effective_tflops": round(info["flops"] / (batch_ms * 1e-3) / 1e12, 2),
+        "per_call": {"device_ms": round(percall_ms, 3), "wall_ms": round(percall_wall_ms, 3),
+                     "solves_per_s_wall": round(n / (max(percall_ms, percall_wall_ms) * 1e-3), 1)},
+        "speedup_vs_per_call": round(max(percall_ms, percall_wall_ms) / batch_ms, 2),
+        "autotune_s": round(tune_s, 2), "graph": True, "clocks": clk,
     }
     print(json.dumps(line))
     return 0

@@ -86,6 +86,13 @@ EXTRA = {
     "exoblas_ddot_device": ("i", "ipipip"),
     "exoblas_dsdot_device": ("i", "ipipip"),
     "exoblas_sgemv_noalloc": ("i", "iiiifpipifpip"),
+    "exoblas_batch_plan_create": ("i", "pip"),
+    "exoblas_batch_plan_run": ("i", "p"),
+    "exoblas_batch_plan_graph_launch": ("i", "p"),
+    "exoblas_batch_plan_info": ("i", "pppp"),
+    "exoblas_batch_plan_destroy": ("i", "p"),
+    "exoblas_batch_tune": ("i", ""),
+    "exoblas_batch_tile_config": ("i", "iii"),
 }
 
 SIGNATURES = {**L1, **L2, **L3, **EXTRA}

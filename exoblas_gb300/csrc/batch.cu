@@ -1,0 +1,680 @@
+// Batched execution of many independent, unevenly sized BLAS calls in one
+// persistent launch: sgemm, dgemv and strsv (the reference's exo_sgemm,
+// exo_dgemv and exo_strsv semantics, test/level3/gemm/exo_gemm_wrapper.h,
+// test/level2/gemv/exo_gemv_wrapper.h, test/level2/trsv/exo_trsv_wrapper.h).
+//
+// A plan turns the calls into work units, each small enough for one CTA:
+//   GEMM_TILE   one TM x TN tile of one sgemm, TM x TN chosen per call by the
+//               autotuner (32x32, 64x64 or 128x128)
+//   GEMV_ROWS   128 rows of a NoTrans dgemv / 64 columns of a Trans dgemv
+//   TRSV        one whole strsv (blocked substitution inside the CTA)
+// sorted longest-first (each unit's cost estimated from its flops and bytes)
+// and uploaded once.  A run zeroes a ticket and launches the persistent
+// kernel (grid = SMs x resident CTAs), whose CTAs claim units in order with
+// atomicAdd.  Runs are capturable in a CUDA graph (exoblas_batch_graph).
+// The autotuner measures each tile shape's saturated throughput per K
+// bucket and picks, per call, the shape with the least estimated time
+// (padding waste included); measurements are cached in a JSON file when
+// EXOBLAS_TUNE_CACHE names one.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "runtime.h"
+
+namespace exb {
+namespace bt {
+
+constexpr int kThreads = 256;
+
+enum UnitKind : int { kGemmTile = 0, kGemvRows = 1, kGemvCols = 2, kTrsv = 3 };
+
+struct Unit {
+  int kind;
+  int op;      // index into the op table
+  int r0, c0;  // tile / strip origin
+  int cfg;     // gemm tile config
+};
+
+struct Op {  // device copy of exoblas_batch_op, normalised
+  int op;
+  int f0, f1, f2;
+  int m, n, k;
+  double alpha, beta;
+  const void *A;
+  long lda;
+  const void *B;
+  long ldb;
+  void *C;
+  long ldc;
+};
+
+// ------------------------------------------------------------ gemm tiles --
+// One TM x TN tile of C = alpha op(A) op(B) + beta C: RM x RN outputs per
+// thread, 16-deep K slices double-buffered in shared memory with the next
+// slice prefetched into registers while the current one is multiplied.
+template <int TM, int TN, int RM, int RN>
+__device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
+  constexpr int BK = 16;
+  constexpr int TX = TN / RN, TY = TM / RM;
+  constexpr int LA = BK * TM / kThreads, LB = BK * TN / kThreads;
+  static_assert(TX * TY == kThreads, "tile shape");
+  float *As = sm, *Bs = sm + 2 * BK * TM;  // [2][BK][TM], [2][BK][TN]
+  const float *A = static_cast<const float *>(o.A), *B = static_cast<const float *>(o.B);
+  float *C = static_cast<float *>(o.C);
+  const bool ta = o.f0 != 111, tb = o.f1 != 111;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  float ra[LA], rb[LB];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int s = 0; s < LA; ++s) {
+      const int e = threadIdx.x + s * kThreads;
+      const int kk = ta ? e / TM : e % BK, i = ta ? e % TM : e / BK;
+      const long gi = m0 + i, gk = k0 + kk;
+      ra[s] = (gi < o.m && gk < o.k) ? (ta ? A[gk * o.lda + gi] : A[gi * o.lda + gk]) : 0.f;
+    }
+#pragma unroll
+    for (int s = 0; s < LB; ++s) {
+      const int e = threadIdx.x + s * kThreads;
+      const int kk = tb ? e % BK : e / TN, j = tb ? e / BK : e % TN;
+      const long gj = n0 + j, gk = k0 + kk;
+      rb[s] = (gj < o.n && gk < o.k) ? (tb ? B[gj * o.ldb + gk] : B[gk * o.ldb + gj]) : 0.f;
+    }
+  };
+  auto stash = [&](int buf) {
+#pragma unroll
+    for (int s = 0; s < LA; ++s) {
+      const int e = threadIdx.x + s * kThreads;
+      const int kk = ta ? e / TM : e % BK, i = ta ? e % TM : e / BK;
+      As[(buf * BK + kk) * TM + i] = ra[s];
+    }
+#pragma unroll
+    for (int s = 0; s < LB; ++s) {
+      const int e = threadIdx.x + s * kThreads;
+      const int kk = tb ? e % BK : e / TN, j = tb ? e / BK : e % TN;
+      Bs[(buf * BK + kk) * TN + j] = rb[s];
+    }
+  };
+  float acc[RM][RN];
+#pragma unroll
+  for (int i = 0; i < RM; ++i)
+#pragma unroll
+    for (int j = 0; j < RN; ++j) acc[i][j] = 0.f;
+  __syncthreads();  // the previous unit may still read shared memory
+  fetch(0);
+  stash(0);
+  __syncthreads();
+  int buf = 0;
+  for (int k0 = 0; k0 < o.k; k0 += BK) {
+    const bool more = k0 + BK < o.k;
+    if (more) fetch(k0 + BK);
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      float a[RM], b[RN];
+#pragma unroll
+      for (int i = 0; i < RM; ++i) a[i] = As[(buf * BK + kk) * TM + ty * RM + i];
+#pragma unroll
+      for (int j = 0; j < RN; ++j) b[j] = Bs[(buf * BK + kk) * TN + tx + j * TX];
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    if (more) stash(buf ^ 1);
+    buf ^= 1;
+    __syncthreads();
+  }
+  const float alpha = float(o.alpha), beta = float(o.beta);
+#pragma unroll
+  for (int i = 0; i < RM; ++i) {
+    const long gi = m0 + ty * RM + i;
+    if (gi >= o.m) continue;
+#pragma unroll
+    for (int j = 0; j < RN; ++j) {
+      const long gj = n0 + tx + j * TX;
+      if (gj >= o.n) continue;
+      float *c = C + gi * o.ldc + gj;
+      *c = alpha * acc[i][j] + beta * *c;
+    }
+  }
+}
+
+// -------------------------------------------------------------- gemv -------
+// NoTrans: rows [r0, r0+128) of y = beta y + alpha A x, a warp per row.
+__device__ void gemv_rows(const Op &o, int r0) {
+  const double *A = static_cast<const double *>(o.A), *x = static_cast<const double *>(o.B);
+  double *y = static_cast<double *>(o.C);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long incx = o.ldb, incy = o.ldc;
+  const double *xb = incx < 0 ? x + (1 - long(o.n)) * incx : x;
+  double *yb = incy < 0 ? y + (1 - long(o.m)) * incy : y;
+  for (int r = r0 + warp; r < r0 + 128 && r < o.m; r += kThreads / 32) {
+    const double *a = A + long(r) * o.lda;
+    double s0 = 0, s1 = 0;
+    int j = lane;
+    for (; j + 32 < o.n; j += 64) {
+      s0 = fma(a[j], xb[j * incx], s0);
+      s1 = fma(a[j + 32], xb[(j + 32) * incx], s1);
+    }
+    if (j < o.n) s0 = fma(a[j], xb[j * incx], s0);
+    double s = s0 + s1;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if (lane == 0) {
+      double *yr = yb + long(r) * incy;
+      *yr = o.alpha * s + o.beta * *yr;
+    }
+  }
+}
+// Trans: columns [c0, c0+64) of y = beta y + alpha A^T x (A is m x n,
+// y has n entries).  Lane quad q = tid / 4 owns column c0 + q; its four
+// lanes take rows i = 4t + (tid % 4) and combine with two shuffles in a
+// fixed order, so no shared memory or block barrier is involved.
+__device__ void gemv_cols(const Op &o, int c0) {
+  const double *A = static_cast<const double *>(o.A), *x = static_cast<const double *>(o.B);
+  double *y = static_cast<double *>(o.C);
+  const long incx = o.ldb, incy = o.ldc;
+  const double *xb = incx < 0 ? x + (1 - long(o.m)) * incx : x;
+  double *yb = incy < 0 ? y + (1 - long(o.n)) * incy : y;
+  const int col = threadIdx.x >> 2, grp = threadIdx.x & 3;
+  const long j = c0 + col;
+  double s = 0;
+  if (j < o.n)
+    for (int i = grp; i < o.m; i += 4) s = fma(A[long(i) * o.lda + j], xb[i * incx], s);
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  if (grp == 0 && j < o.n) {
+    double *yj = yb + j * incy;
+    *yj = o.alpha * s + o.beta * *yj;
+  }
+}
+
+// -------------------------------------------------------------- trsv -------
+// One whole strsv in one CTA: 32-row blocks; the 8 warps update the next
+// block's right-hand side with the solved prefix (row dots), then warp 0
+// substitutes through the 32 x 32 diagonal block with shuffles.  Effective
+// lower formulation as in trsv.cu.
+__device__ void trsv_cta(const Op &o, float *sm) {
+  const float *A = static_cast<const float *>(o.A);
+  float *x = static_cast<float *>(o.C);
+  const long n = o.m, lda = o.lda, inc = o.ldc;
+  float *xb = inc < 0 ? x + (1 - n) * inc : x;
+  const bool upper = o.f0 == 121, trans = o.f1 != 111, unit = o.f2 != 131;
+  const bool rev = upper != trans;
+  auto cidx = [&](long k) { return rev ? n - 1 - k : k; };
+  auto L = [&](long i, long j) -> float {
+    const long ci = cidx(i), cj = cidx(j);
+    return trans ? A[cj * lda + ci] : A[ci * lda + cj];
+  };
+  float *z = sm;  // solved values in effective order (n <= 4096)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long b0 = 0; b0 < n; b0 += 32) {
+    const long rows = n - b0 < 32 ? n - b0 : 32;
+    // rhs for the block: b - L[b0.., 0:b0] z[0:b0], four rows per warp
+    for (int r = warp; r < rows; r += kThreads / 32) {
+      const long i = b0 + r;
+      float s = 0.f;
+      for (long j = lane; j < b0; j += 32) s = fmaf(L(i, j), z[j], s);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) z[i] = xb[cidx(i) * inc] - s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      float v = lane < rows ? z[b0 + lane] : 0.f;
+      for (int j = 0; j < rows; ++j) {
+        float xj = v;
+        if (lane == j && !unit) xj = v / L(b0 + j, b0 + j);
+        xj = __shfl_sync(0xffffffffu, xj, j);
+        if (lane == j) v = xj;
+        if (lane > j && lane < rows) v = fmaf(-L(b0 + lane, b0 + j), xj, v);
+      }
+      if (lane < rows) z[b0 + lane] = v;
+    }
+    __syncthreads();
+  }
+  for (long i = threadIdx.x; i < n; i += kThreads) xb[cidx(i) * inc] = z[i];
+}
+
+// ---------------------------------------------------------------- kernel --
+__global__ void __launch_bounds__(kThreads)
+    batch_kernel(const Op *__restrict__ ops, const Unit *__restrict__ units, int nunits, int *ticket) {
+  extern __shared__ __align__(16) float smem_f[];
+  __shared__ int s_u;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_u = atomicAdd(ticket, 1);
+    __syncthreads();
+    const int u = s_u;
+    if (u >= nunits) return;
+    const Unit un = units[u];
+    const Op o = ops[un.op];
+    switch (un.kind) {
+      case kGemmTile:
+        if (un.cfg == 0)
+          gemm_tile<32, 32, 2, 2>(o, un.r0, un.c0, smem_f);
+        else if (un.cfg == 1)
+          gemm_tile<64, 64, 4, 4>(o, un.r0, un.c0, smem_f);
+        else
+          gemm_tile<128, 128, 8, 8>(o, un.r0, un.c0, smem_f);
+        break;
+      case kGemvRows:
+        gemv_rows(o, un.r0);
+        break;
+      case kGemvCols:
+        gemv_cols(o, un.c0);
+        break;
+      default:
+        trsv_cta(o, smem_f);
+        break;
+    }
+  }
+}
+
+constexpr size_t kSmem = 2 * 16 * (128 + 128) * 4 > 4096 * 4 ? 2 * 16 * (128 + 128) * 4 : 4096 * 4;
+
+// --------------------------------------------------------------- tuner -----
+// The autotuner measures, for every tile shape and K bucket (K = 16 * 2^b),
+// the saturated throughput of that tile shape: one launch of enough tiles to
+// fill every SM (a 2048 x 2048 output), timed with CUDA events after a
+// warm-up.  A call (m, n, k) then gets the shape minimising
+//   ceil(m / TM) ceil(n / TN) TM TN k / throughput(shape, bucket(k)),
+// i.e. measured speed with the padding waste of the shape counted in.
+const int kTiles[3][2] = {{32, 32}, {64, 64}, {128, 128}};
+
+static int bucket(int v) {
+  int b = 0;
+  while (b < 7 && (16 << (b + 1)) <= v) ++b;
+  return b;  // 16..31 -> 0, ..., >= 2048 -> 7
+}
+
+struct Tuner {
+  std::mutex mu;
+  bool loaded = false;
+  bool tuned = false;
+  double gflops[3][8];  // measured throughput per [tile shape][K bucket]
+  Tuner() {
+    // untuned defaults (GFLOP/s): larger tiles reuse more per byte
+    for (int b = 0; b < 8; ++b) {
+      gflops[0][b] = 6000;
+      gflops[1][b] = 14000;
+      gflops[2][b] = 22000;
+    }
+  }
+};
+static Tuner g_tuner;
+
+static const char *cache_path() {
+  const char *p = getenv("EXOBLAS_TUNE_CACHE");
+  return p && *p ? p : nullptr;
+}
+
+// cache format: {"batch_sgemm_gflops": [[t00, ..., t07], [t10, ...], [t20, ...]]}
+static void load_cache() {
+  if (g_tuner.loaded) return;
+  g_tuner.loaded = true;
+  const char *path = cache_path();
+  if (!path) return;
+  FILE *f = fopen(path, "r");
+  if (!f) return;
+  char buf[4096];
+  const size_t nr = fread(buf, 1, sizeof buf - 1, f);
+  fclose(f);
+  buf[nr] = 0;
+  const char *p = strstr(buf, "batch_sgemm_gflops");
+  if (!p) return;
+  double v[3][8];
+  for (int i = 0; i < 3; ++i) {
+    p = strchr(p + 1, '[');
+    if (!p) return;
+    if (i == 0) {
+      p = strchr(p + 1, '[');
+      if (!p) return;
+    }
+    ++p;
+    for (int j = 0; j < 8; ++j) {
+      char *end = nullptr;
+      v[i][j] = strtod(p, &end);
+      if (end == p || !(v[i][j] > 0)) return;
+      p = end;
+      while (*p == ',' || *p == ' ') ++p;
+    }
+  }
+  memcpy(g_tuner.gflops, v, sizeof v);
+  g_tuner.tuned = true;
+}
+
+static void save_cache() {
+  const char *path = cache_path();
+  if (!path) return;
+  FILE *f = fopen(path, "w");
+  if (!f) return;
+  fprintf(f, "{\"batch_sgemm_gflops\": [");
+  for (int i = 0; i < 3; ++i) {
+    fprintf(f, "%s[", i ? ", " : "");
+    for (int j = 0; j < 8; ++j) fprintf(f, "%s%.1f", j ? ", " : "", g_tuner.gflops[i][j]);
+    fprintf(f, "]");
+  }
+  fprintf(f, "]}\n");
+  fclose(f);
+}
+
+static int launch_units(const Op *dops, const Unit *dunits, int nunits, int *ticket, cudaStream_t s, int sms);
+
+static void tune_all() {
+  Context &c = ctx();
+  const int d = 2048, kmax = 2048;
+  float *a = nullptr, *b = nullptr, *cm = nullptr;
+  Op *dop = nullptr;
+  Unit *du = nullptr;
+  int *tk = nullptr;
+  const int maxunits = (d / 32) * (d / 32);
+  EXB_CUDA(cudaMalloc(&a, size_t(d) * kmax * 4));
+  EXB_CUDA(cudaMalloc(&b, size_t(d) * kmax * 4));
+  EXB_CUDA(cudaMalloc(&cm, size_t(d) * d * 4));
+  EXB_CUDA(cudaMalloc(&dop, sizeof(Op)));
+  EXB_CUDA(cudaMalloc(&du, sizeof(Unit) * maxunits));
+  EXB_CUDA(cudaMalloc(&tk, 4));
+  EXB_CUDA(cudaMemsetAsync(a, 0, size_t(d) * kmax * 4, c.stream));
+  EXB_CUDA(cudaMemsetAsync(b, 0, size_t(d) * kmax * 4, c.stream));
+  cudaEvent_t e0, e1;
+  EXB_CUDA(cudaEventCreate(&e0));
+  EXB_CUDA(cudaEventCreate(&e1));
+  std::vector<Unit> us;
+  for (int cf = 0; cf < 3; ++cf) {
+    const int TM = kTiles[cf][0], TN = kTiles[cf][1];
+    us.clear();
+    for (int i = 0; i < d; i += TM)
+      for (int j = 0; j < d; j += TN) us.push_back(Unit{kGemmTile, 0, i, j, cf});
+    EXB_CUDA(cudaMemcpyAsync(du, us.data(), sizeof(Unit) * us.size(), cudaMemcpyHostToDevice, c.stream));
+    for (int bk = 0; bk < 8; ++bk) {
+      const int kk = 16 << bk;
+      Op o{};
+      o.op = 1;
+      o.f0 = o.f1 = 111;
+      o.m = o.n = d;
+      o.k = kk;
+      o.alpha = 1;
+      o.beta = 0;
+      o.A = a;
+      o.lda = kk;
+      o.B = b;
+      o.ldb = d;
+      o.C = cm;
+      o.ldc = d;
+      EXB_CUDA(cudaMemcpyAsync(dop, &o, sizeof o, cudaMemcpyHostToDevice, c.stream));
+      launch_units(dop, du, int(us.size()), tk, c.stream, c.sm_count);  // warm-up
+      EXB_CUDA(cudaEventRecord(e0, c.stream));
+      launch_units(dop, du, int(us.size()), tk, c.stream, c.sm_count);
+      EXB_CUDA(cudaEventRecord(e1, c.stream));
+      EXB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      EXB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      g_tuner.gflops[cf][bk] = 2.0 * d * double(d) * kk / (double(ms) * 1e-3) / 1e9;
+    }
+  }
+  g_tuner.tuned = true;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(a);
+  cudaFree(b);
+  cudaFree(cm);
+  cudaFree(dop);
+  cudaFree(du);
+  cudaFree(tk);
+  save_cache();
+}
+
+static int tile_config(int m, int n, int k) {
+  std::lock_guard<std::mutex> lk(g_tuner.mu);
+  load_cache();
+  const int bk = bucket(k > 0 ? k : 1);
+  int best = 0;
+  double best_t = 1e300;
+  for (int cf = 0; cf < 3; ++cf) {
+    const double TM = kTiles[cf][0], TN = kTiles[cf][1];
+    const double work = std::ceil(m / TM) * std::ceil(n / TN) * TM * TN * double(k > 0 ? k : 1) * 2.0;
+    const double t = work / (g_tuner.gflops[cf][bk] * 1e9);
+    if (t < best_t * 0.98) {  // prefer the larger tile on near-ties
+      best_t = t;
+      best = cf;
+    } else if (t < best_t * 1.02) {
+      best = cf;
+      best_t = std::min(best_t, t);
+    }
+  }
+  return best;
+}
+
+static int launch_units(const Op *dops, const Unit *dunits, int nunits, int *ticket, cudaStream_t s, int sms) {
+  static bool attr[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr[dev]) {
+    EXB_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kSmem)));
+    attr[dev] = true;
+  }
+  int per_sm = 0;
+  EXB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, kThreads, kSmem));
+  int grid = sms * (per_sm > 0 ? per_sm : 1);
+  if (grid > nunits) grid = nunits;
+  if (grid < 1) return 0;
+  EXB_CUDA(cudaMemsetAsync(ticket, 0, 4, s));
+  batch_kernel<<<grid, kThreads, kSmem, s>>>(dops, dunits, nunits, ticket);
+  EXB_LAUNCH("batch kernel");
+  count_launch();
+  return grid;
+}
+
+// ------------------------------------------------------------------ plan ---
+struct Plan {
+  int device = 0;
+  Op *ops = nullptr;
+  Unit *units = nullptr;
+  int *ticket = nullptr;
+  int nunits = 0, nops = 0;
+  double flops = 0, bytes = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t graph_stream = nullptr;
+};
+
+static double unit_cost(const exoblas_batch_op &b, int kind, int cfg) {
+  // seconds-like score: flops at ~40 TF/s FP32, bytes at ~6 TB/s, trsv chain
+  switch (kind) {
+    case kGemmTile: {
+      const double t = kTiles[cfg][0] * double(kTiles[cfg][1]);
+      return 2.0 * t * b.k / 4e13 + 1e-6;
+    }
+    case kGemvRows:
+      return 128.0 * b.n * 8 / 6e12 + 1e-6;
+    case kGemvCols:
+      return 64.0 * b.m * 8 / 6e12 + 1e-6;
+    default:
+      return double(b.m) * b.m / 2 / 5e10 + b.m * 5e-8;  // one CTA, FP32 chain
+  }
+}
+
+}  // namespace bt
+}  // namespace exb
+
+using namespace exb;
+
+extern "C" {
+
+int exoblas_batch_tune(void) {
+  return guarded("exoblas_batch_tune", [&] {
+    std::lock_guard<std::mutex> lk(bt::g_tuner.mu);
+    bt::load_cache();
+    bt::tune_all();
+  });
+}
+
+int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_batch_plan *out) {
+  return guarded("exoblas_batch_plan_create", [&] {
+    if (!out) fail(EXOBLAS_INVALID_VALUE, "plan pointer is NULL");
+    *out = nullptr;
+    if (count < 0 || (count > 0 && !ops)) fail(EXOBLAS_INVALID_VALUE, "bad op list");
+    Context &c = ctx();
+    std::vector<bt::Op> dops(count);
+    std::vector<std::pair<double, bt::Unit>> us;
+    double flops = 0, bytes = 0;
+    for (int i = 0; i < count; ++i) {
+      const exoblas_batch_op &b = ops[i];
+      bt::Op &o = dops[i];
+      o.op = b.op;
+      o.f0 = b.flags[0];
+      o.f1 = b.flags[1];
+      o.f2 = b.flags[2];
+      o.m = b.m;
+      o.n = b.n;
+      o.k = b.k;
+      o.alpha = b.alpha;
+      o.beta = b.beta;
+      o.A = b.A;
+      o.lda = b.lda;
+      o.B = b.B;
+      o.ldb = b.ldb;
+      o.C = b.C;
+      o.ldc = b.ldc;
+      if (b.m < 0 || b.n < 0 || b.k < 0) fail(EXOBLAS_INVALID_VALUE, "negative size in a batch op");
+      for (const void *p : {b.A, b.B, static_cast<const void *>(b.C)})
+        if (p && !is_device_pointer(p)) fail(EXOBLAS_INVALID_VALUE, "batch operands must be device pointers");
+      switch (b.op) {
+        case EXOBLAS_BATCH_SGEMM: {
+          if (b.m == 0 || b.n == 0) break;
+          const int cf = bt::tile_config(b.m, b.n, b.k);
+          const int TM = bt::kTiles[cf][0], TN = bt::kTiles[cf][1];
+          for (int r = 0; r < b.m; r += TM)
+            for (int cc = 0; cc < b.n; cc += TN)
+              us.push_back({bt::unit_cost(b, bt::kGemmTile, cf), bt::Unit{bt::kGemmTile, i, r, cc, cf}});
+          flops += 2.0 * b.m * b.n * b.k;
+          break;
+        }
+        case EXOBLAS_BATCH_DGEMV: {
+          if (b.m == 0 || b.n == 0) break;
+          if (b.ldb == 0 || b.ldc == 0) fail(EXOBLAS_INVALID_VALUE, "zero vector stride in a batch dgemv");
+          if (b.flags[0] == 111) {
+            for (int r = 0; r < b.m; r += 128)
+              us.push_back({bt::unit_cost(b, bt::kGemvRows, 0), bt::Unit{bt::kGemvRows, i, r, 0, 0}});
+          } else {
+            for (int cc = 0; cc < b.n; cc += 64)
+              us.push_back({bt::unit_cost(b, bt::kGemvCols, 0), bt::Unit{bt::kGemvCols, i, 0, cc, 0}});
+          }
+          bytes += (double(b.m) * b.n + b.m + 2.0 * b.n) * 8;
+          break;
+        }
+        case EXOBLAS_BATCH_STRSV: {
+          if (b.m == 0) break;
+          if (b.m > 4096) fail(EXOBLAS_INVALID_VALUE, "batch strsv supports N <= 4096");
+          if (b.ldc == 0) fail(EXOBLAS_INVALID_VALUE, "zero stride in a batch strsv");
+          us.push_back({bt::unit_cost(b, bt::kTrsv, 0), bt::Unit{bt::kTrsv, i, 0, 0, 0}});
+          bytes += (double(b.m) * (b.m + 1) / 2 + 2.0 * b.m) * 4;
+          break;
+        }
+        default:
+          fail(EXOBLAS_INVALID_VALUE, "unknown batch op");
+      }
+    }
+    // longest first; ties keep submission order (stable)
+    std::stable_sort(us.begin(), us.end(),
+                     [](const std::pair<double, bt::Unit> &a, const std::pair<double, bt::Unit> &b) {
+                       return a.first > b.first;
+                     });
+    std::vector<bt::Unit> units(us.size());
+    for (size_t i = 0; i < us.size(); ++i) units[i] = us[i].second;
+    bt::Plan *p = new bt::Plan();
+    p->device = c.device;
+    p->nops = count;
+    p->nunits = int(units.size());
+    p->flops = flops;
+    p->bytes = bytes;
+    cudaError_t e = cudaMalloc(&p->ops, sizeof(bt::Op) * (count ? count : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&p->units, sizeof(bt::Unit) * (units.empty() ? 1 : units.size()));
+    if (e == cudaSuccess) e = cudaMalloc(&p->ticket, 256);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(p->ops);
+      cudaFree(p->units);
+      cudaFree(p->ticket);
+      delete p;
+      fail(EXOBLAS_ALLOC_FAILED, "batch plan allocation failed");
+    }
+    EXB_CUDA(cudaMemcpyAsync(p->ops, dops.data(), sizeof(bt::Op) * count, cudaMemcpyHostToDevice, c.stream));
+    if (!units.empty())
+      EXB_CUDA(cudaMemcpyAsync(p->units, units.data(), sizeof(bt::Unit) * units.size(), cudaMemcpyHostToDevice,
+                               c.stream));
+    EXB_CUDA(cudaStreamSynchronize(c.stream));
+    *out = reinterpret_cast<exoblas_batch_plan>(p);
+  });
+}
+
+int exoblas_batch_plan_run(exoblas_batch_plan plan) {
+  return guarded("exoblas_batch_plan_run", [&] {
+    bt::Plan *p = reinterpret_cast<bt::Plan *>(plan);
+    if (!p) fail(EXOBLAS_INVALID_VALUE, "NULL plan");
+    Context &c = ctx();
+    if (c.device != p->device) fail(EXOBLAS_INVALID_VALUE, "plan belongs to another device");
+    bt::launch_units(p->ops, p->units, p->nunits, p->ticket, c.stream, c.sm_count);
+    if (c.blocking) EXB_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int exoblas_batch_plan_graph_launch(exoblas_batch_plan plan) {
+  return guarded("exoblas_batch_plan_graph_launch", [&] {
+    bt::Plan *p = reinterpret_cast<bt::Plan *>(plan);
+    if (!p) fail(EXOBLAS_INVALID_VALUE, "NULL plan");
+    Context &c = ctx();
+    if (!p->exec) {
+      // capture one run (ticket reset + persistent kernel) on a private stream
+      EXB_CUDA(cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking));
+      EXB_CUDA(cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal));
+      bt::launch_units(p->ops, p->units, p->nunits, p->ticket, p->graph_stream, c.sm_count);
+      EXB_CUDA(cudaStreamEndCapture(p->graph_stream, &p->graph));
+      EXB_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+    }
+    EXB_CUDA(cudaGraphLaunch(p->exec, c.stream));
+    if (c.blocking) EXB_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int exoblas_batch_plan_info(exoblas_batch_plan plan, int *units, double *flops, double *bytes) {
+  return guarded("exoblas_batch_plan_info", [&] {
+    bt::Plan *p = reinterpret_cast<bt::Plan *>(plan);
+    if (!p) fail(EXOBLAS_INVALID_VALUE, "NULL plan");
+    if (units) *units = p->nunits;
+    if (flops) *flops = p->flops;
+    if (bytes) *bytes = p->bytes;
+  });
+}
+
+int exoblas_batch_plan_destroy(exoblas_batch_plan plan) {
+  return guarded("exoblas_batch_plan_destroy", [&] {
+    bt::Plan *p = reinterpret_cast<bt::Plan *>(plan);
+    if (!p) return;
+    cudaStreamSynchronize(ctx().stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->graph_stream) cudaStreamDestroy(p->graph_stream);
+    cudaFree(p->ops);
+    cudaFree(p->units);
+    cudaFree(p->ticket);
+    delete p;
+  });
+}
+
+int exoblas_batch_tile_config(int m, int n, int k) {
+  int c = -1;
+  guarded("exoblas_batch_tile_config", [&] { c = bt::tile_config(m, n, k); });
+  return c;
+}
+
+}  // extern "C"

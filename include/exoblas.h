@@ -221,6 +221,43 @@ EXOBLAS_API void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO U
                const int K, const double alpha, const double *A, const int lda, const double beta, double *C,
                const int ldc);
 
+/* ------------------------------------------------------------ batching --- */
+/* Many independent exo_sgemm / exo_dgemv / exo_strsv calls of uneven sizes
+ * in one persistent launch (no counterpart in the reference, whose calls run
+ * one at a time on the calling thread).  All operands are device pointers.
+ *   SGEMM: flags = {TransA, TransB}, m, n, k, alpha, beta, A/lda, B/ldb, C/ldc (float)
+ *   DGEMV: flags = {TransA}, m = M, n = N, alpha, beta, A/lda, B = X (ldb = incX),
+ *          C = Y (ldc = incY) (double)
+ *   STRSV: flags = {Uplo, TransA, Diag}, m = N (<= 4096), A/lda, C = X (ldc = incX) (float)
+ * Semantics per call are those of the corresponding exo_* entry point.  A
+ * plan uploads the calls once; runs queue one persistent kernel on the
+ * thread's stream (blocking mode waits for it); graph launches replay a
+ * captured CUDA graph of that run.  sgemm tile shapes come from the
+ * autotuner (exoblas_batch_tune; cached in the JSON file named by
+ * EXOBLAS_TUNE_CACHE when set). */
+enum EXOBLAS_BATCH_OPCODE { EXOBLAS_BATCH_SGEMM = 1, EXOBLAS_BATCH_DGEMV = 2, EXOBLAS_BATCH_STRSV = 3 };
+typedef struct exoblas_batch_op {
+  int op;
+  int flags[3];
+  int m, n, k;
+  double alpha, beta;
+  const void *A;
+  int lda;
+  const void *B;
+  int ldb;
+  void *C;
+  int ldc;
+} exoblas_batch_op;
+typedef struct exoblas_batch_plan_s *exoblas_batch_plan;
+EXOBLAS_API int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_batch_plan *plan);
+EXOBLAS_API int exoblas_batch_plan_run(exoblas_batch_plan plan);
+EXOBLAS_API int exoblas_batch_plan_graph_launch(exoblas_batch_plan plan);
+EXOBLAS_API int exoblas_batch_plan_info(exoblas_batch_plan plan, int *units, double *flops, double *bytes);
+EXOBLAS_API int exoblas_batch_plan_destroy(exoblas_batch_plan plan);
+EXOBLAS_API int exoblas_batch_tune(void);
+/* tile configuration the autotuner picked for an sgemm of this shape (0: 32x32, 1: 64x64, 2: 128x128) */
+EXOBLAS_API int exoblas_batch_tile_config(int m, int n, int k);
+
 #ifdef __cplusplus
 }
 #endif

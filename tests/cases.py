@@ -182,12 +182,12 @@ def trmv_cases(p, Ns=(2, 100, 321)):
                    label=f"u={u} t={t} d={d} n={n} lda={lda} inc={ix}")
 
 
-def trsv_cases(p, Ns=(2, 100, 321), fixture=False):
+def trsv_cases(p, Ns=(2, 100, 321), fixture=False, incs=(1, 2, -2), ldds=(0, 5)):
     """test/level2/trsv/correctness.cpp:42-58.  fixture=True reproduces the
     reference's deterministic inputs (A[i*lda+j] = 2 + j/N in integer
     arithmetic, i.e. all 2.0; X[i] = i, :20-25); otherwise A is
     well-conditioned (off-diagonal uniform[-1,1)/n, diagonal 1 + uniform[0,1))."""
-    for u, t, d, n, ix, ldd in itertools.product((UP, LO), (NT, TR), (UN, NU), Ns, (1, 2, -2), (0, 5)):
+    for u, t, d, n, ix, ldd in itertools.product((UP, LO), (NT, TR), (UN, NU), Ns, incs, ldds):
         lda = n + ldd
         if fixture:
             if ix < 0:

@@ -1,0 +1,119 @@
+"""Batched persistent execution: every instance of a mixed batch must match
+the CPU oracle for the same call (1% rule and componentwise FP bound), alone
+and inside the batch, for plain runs and CUDA-graph replays."""
+import numpy as np
+import pytest
+
+from common import EPS, LO, NT, NU, ROW, TR, UN, UP, Case, assert_bound, assert_rel1pct, fp64_reference, run_oracle
+
+
+def _mixed_cases(seed=3, count=60):
+    g = np.random.default_rng(seed)
+    cases = []
+    for i in range(count):
+        kind = i % 3
+        m, n, k = (int(v) for v in np.exp(g.uniform(0, np.log(300), 3)).astype(int).clip(1, 300))
+        if kind == 0:
+            ta, tb = (NT, TR)[i % 2], (NT, TR)[(i // 2) % 2]
+            ar, ac = (m, k) if ta == NT else (k, m)
+            br, bc = (k, n) if tb == NT else (n, k)
+            A = g.uniform(-1, 1, ar * ac).astype(np.float32)
+            B = g.uniform(-1, 1, br * bc).astype(np.float32)
+            Cm = g.uniform(-1, 1, m * n).astype(np.float32)
+            cases.append(Case("sgemm", [ROW, ta, tb, m, n, k, 1.5, A, ac, B, bc, 0.5, Cm, n], [12], nred=k + 1))
+        elif kind == 1:
+            t = (NT, TR)[i % 2]
+            incx, incy = (1, 2, -1)[i % 3], (1, -2)[i % 2]
+            xl, yl = (n, m) if t == NT else (m, n)
+            A = g.uniform(-1, 1, m * n)
+            x = g.uniform(-1, 1, 1 + (xl - 1) * abs(incx))
+            y = g.uniform(-1, 1, 1 + (yl - 1) * abs(incy))
+            cases.append(Case("dgemv", [ROW, t, m, n, 0.75, A, n, x, incx, 0.5, y, incy], [10], nred=xl + 1))
+        else:
+            u, t, d = (UP, LO)[i % 2], (NT, TR)[(i // 2) % 2], (NU, UN)[(i // 4) % 2]
+            A = g.uniform(-1, 1, (m, m)) / m
+            A[np.arange(m), np.arange(m)] = 1 + g.uniform(0, 1, m)
+            x = g.uniform(-1, 1, m)
+            cases.append(Case("strsv", [ROW, u, t, d, m, A.astype(np.float32).ravel(), m, x.astype(np.float32), 1],
+                              [7], nred=m + 1))
+    return cases
+
+
+def _to_ops(torch, cases):
+    from exoblas_gb300.batch import BatchOp
+
+    ops, dev = [], []
+    for c in cases:
+        a = [torch.from_numpy(v.copy()).cuda() if isinstance(v, np.ndarray) else v for v in c.args]
+        dev.append(a)
+        if c.op == "sgemm":
+            _, ta, tb, m, n, k, al, A, lda, B, ldb, be, Cm, ldc = a
+            ops.append(BatchOp.sgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, Cm, ldc))
+        elif c.op == "dgemv":
+            _, t, m, n, al, A, lda, x, ix, be, y, iy = a
+            ops.append(BatchOp.dgemv(t, m, n, al, A, lda, x, ix, be, y, iy))
+        else:
+            _, u, t, d, n, A, lda, x, ix = a
+            ops.append(BatchOp.strsv(u, t, d, n, A, lda, x, ix))
+    return ops, dev
+
+
+def _check(case, got):
+    o_r, o_a = run_oracle(case)
+    j = case.outputs[0]
+    assert_rel1pct(got, o_a[j], f"batch {case.op}")
+    if case.op == "strsv":
+        return
+    (r64, a64), (m, am) = fp64_reference(case)
+    assert_bound(got, a64[j], am[j], case.nred, case.p, 4.0, f"batch {case.op}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [False, True])
+def test_mixed_batch_matches_oracle(cuda, graph):
+    from exoblas_gb300.batch import BatchPlan
+
+    torch = cuda
+    cases = _mixed_cases()
+    ops, dev = _to_ops(torch, cases)
+    plan = BatchPlan(ops)
+    assert plan.info()["units"] >= len(cases)
+    if graph:
+        plan.graph_launch()
+    else:
+        plan.run()
+    torch.cuda.synchronize()
+    for c, a in zip(cases, dev):
+        _check(c, a[c.outputs[0]].cpu().numpy())
+    plan.close()
+
+
+@pytest.mark.gpu
+def test_batch_result_same_alone_and_in_mix(cuda):
+    """Each instance alone (a one-op plan) equals its value inside the mix."""
+    from exoblas_gb300.batch import BatchPlan
+
+    torch = cuda
+    cases = _mixed_cases(seed=9, count=24)
+    ops, dev = _to_ops(torch, cases)
+    mixed = BatchPlan(ops)
+    mixed.run()
+    torch.cuda.synchronize()
+    outs = [a[c.outputs[0]].cpu().numpy().copy() for c, a in zip(cases, dev)]
+    ops2, dev2 = _to_ops(torch, cases)
+    for i, (c, op) in enumerate(zip(cases, ops2)):
+        p = BatchPlan([op])
+        p.run()
+        torch.cuda.synchronize()
+        alone = dev2[i][c.outputs[0]].cpu().numpy()
+        assert alone.tobytes() == outs[i].tobytes(), f"instance {i} ({c.op}) differs alone vs in the mix"
+        p.close()
+
+
+@pytest.mark.gpu
+def test_autotuner_picks_valid_configs(cuda, tmp_path, monkeypatch):
+    import exoblas_gb300.batch as bt
+
+    monkeypatch.setenv("EXOBLAS_TUNE_CACHE", str(tmp_path / "tune.json"))
+    for m, n, k in [(16, 16, 16), (300, 200, 100), (2048, 2048, 2048)]:
+        assert bt.tile_config(m, n, k) in (0, 1, 2)

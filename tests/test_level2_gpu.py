@@ -111,7 +111,7 @@ def test_dtrsv_full_size_dd(cuda):
     assert fwd.max() <= 64 * n * EPS["d"], fwd.max()
 
 
-CLUSTER = [c for p in "sd" for c in trsv_cases(p, Ns=(1000, 2049, 4160)) if c.args[8] == 1 and c.args[6] == c.args[4]]
+CLUSTER = [c for p in "sd" for c in trsv_cases(p, Ns=(1000, 2049, 4160), incs=(1,), ldds=(0,))]
 
 
 @pytest.mark.gpu
