@@ -69,8 +69,13 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["bandwidth", "precision", "batch"], default="bandwidth",
-                    help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set")
+    ap.add_argument("--workload", choices=["bandwidth", "precision", "batch", "serve"], default="bandwidth",
+                    help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set; batch: "
+                         "4096 mixed instances in one persistent launch; serve: a Poisson request stream")
+    ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=20000.0, help="serve: mean arrivals per second")
+    ap.add_argument("--workers", type=int, default=8, help="serve: server worker streams")
+    ap.add_argument("--per-call-sample", type=int, default=2000, help="serve: requests timed per call")
     ap.add_argument("--size", type=int, default=8192, help="M = N = K of the precision set")
     return ap.parse_args()
 
@@ -297,6 +302,8 @@ def main():
         return run_reference(args)
     if args.workload == "precision":
         return run_precision(args)
+    if args.workload == "serve":
+        return run_serve(args)
     if args.workload == "batch":
         return run_batch(args)
 
@@ -651,6 +658,164 @@ def run_batch(args):
     }
     print(json.dumps(line))
     return 0
+
+
+# ---------------------------------------------------------- serve workload --
+def run_serve(args):
+    """A Poisson request stream (mean args.rate req/s, seed 11) of gemm 60% /
+    gemv 25% / trsv 10% / syrk 5%, every dimension log-uniform in [32, 8192],
+    70% FP32 and 30% FP64 (seed 12), operands resident in HBM, replayed into
+    the request server (split-BF16 for FP32 gemm/syrk, Ozaki for FP64
+    gemm/syrk, admission by free memory).  Baselines on the first
+    args.per_call_sample requests of the same stream, one call after another
+    on one stream (blocking calls, as a CPU BLAS user makes them): plain
+    per-call launches with the native FFMA / DFMA kernels, and per-call with
+    the same precision paths as the server."""
+    import torch
+
+    import exoblas_gb300 as eb
+    from exoblas_gb300 import _native, serve, workloads
+
+    L = _native.lib()
+    torch.cuda.set_device(0)
+    stream = workloads.serve_stream(args.requests, rate=args.rate)
+    ops = workloads.ServeOperands(torch, "cuda")
+    built = [ops.request(op, p, m, n, k) for (_, op, p, m, n, k) in stream]
+    reqs = [b[0] for b in built]
+    offsets = [e[0] for e in stream]
+    torch.cuda.synchronize()
+    work = [workloads.request_work(op, m, n, k, p) for (_, op, p, m, n, k) in stream]
+    reserve = int(2.75 * (1 << 30))  # Ozaki workspace of an 8192^3 dgemm, with the arena's growth margin
+    W = args.workers
+    srv = serve.Server(workers=W, hbm_budget=W * reserve, scratch_reserve=reserve)
+    # warm-up: a short stream of small requests through every path
+    warm = workloads.serve_stream(400, rate=args.rate, seed_arrivals=3, seed_ops=4, hi=1024)
+    wreq = [ops.request(op, p, m, n, k)[0] for (_, op, p, m, n, k) in warm]
+    srv.replay(wreq, [0.0] * len(wreq))
+    srv.drain()
+    srv.close()
+    torch.cuda.synchronize()
+
+    srv = serve.Server(workers=W, hbm_budget=W * reserve, scratch_reserve=reserve)
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.25)
+    t0 = srv.replay(reqs, offsets)
+    srv.drain()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    span = st["completed"] / st["solves_per_s"] if st["solves_per_s"] > 0 else float("nan")
+    flops = sum(w[0] for w in work)
+
+    # per-call baselines on a sample of the same stream
+    vp = C.c_void_p
+
+    def call(r):
+        p, o = r.precision, r.op
+        f, fl = (r.flags[0], r.flags[1], r.flags[2]), None
+        if o == serve.GEMM:
+            fn = L.exo_sgemm if p == 1 else L.exo_dgemm
+            fn(101, f[0], f[1], r.m, r.n, r.k, r.alpha, vp(r.A), r.lda, vp(r.B), r.ldb, r.beta, vp(r.C), r.ldc)
+        elif o == serve.SYRK:
+            fn = L.exo_ssyrk if p == 1 else L.exo_dsyrk
+            fn(101, f[0], f[1], r.m, r.k, r.alpha, vp(r.A), r.lda, r.beta, vp(r.C), r.ldc)
+        elif o == serve.GEMV:
+            fn = L.exo_sgemv if p == 1 else L.exo_dgemv
+            fn(101, f[0], r.m, r.n, r.alpha, vp(r.A), r.lda, vp(r.B), r.ldb, r.beta, vp(r.C), r.ldc)
+        else:
+            fn = L.exo_strsv if p == 1 else L.exo_dtrsv
+            fn(101, f[0], f[1], f[2], r.m, vp(r.A), r.lda, vp(r.C), r.ldc)
+        st_ = L.exoblas_get_status()
+        if st_:
+            raise RuntimeError(f"per-call request failed with status {st_}")
+
+    sample = reqs[:max(1, min(args.per_call_sample, len(reqs)))]
+
+    def per_call(same_paths):
+        eb.set_stream(None)
+        eb.set_blocking(True)
+        lat = []
+        for r in sample[:50]:  # warm
+            eb.set_precision(0 if not same_paths else (1 if r.precision == 1 else 2))
+            call(r)
+        t = time.perf_counter()
+        for r in sample:
+            if same_paths:
+                eb.set_precision(1 if r.precision == 1 else 2)
+            else:
+                eb.set_precision(0)
+            a = time.perf_counter()
+            call(r)
+            lat.append(time.perf_counter() - a)
+        tot = time.perf_counter() - t
+        eb.set_precision(0)
+        eb.set_blocking(False)
+        lat.sort()
+        return {"solves_per_s": round(len(sample) / tot, 1), "seconds": round(tot, 3),
+                "service_p50_ms": round(lat[len(lat) // 2] * 1e3, 3),
+                "service_p99_ms": round(lat[min(len(lat) - 1, int(0.99 * (len(lat) - 1) + 0.5))] * 1e3, 3)}
+
+    base = per_call(False)
+    same = per_call(True)
+    err = serve_errors(torch, eb, call, stream, built)
+    line = {
+        "metric": METRIC, "unit": "solves/s", "value": round(st["solves_per_s"], 1), "higher_is_better": True,
+        "n_gpus": 1, "dtype": "f32 (split-BF16) + f64 (Ozaki)", "data": "synthetic",
+        "config": {"workload": f"serve: Poisson {args.rate:g} req/s (seed 11), gemm 60%/gemv 25%/trsv 10%/syrk 5%, "
+                               "m,n,k log-uniform [32,8192], 70% fp32 / 30% fp64 (seed 12), operands resident",
+                   "requests": len(reqs), "workers": W, "admission_budget_gb": round(W * reserve / 1e9, 1)},
+        "completed": int(st["completed"]), "rejected": int(st["rejected"]), "failed": int(st["failed"]),
+        "p50_ms": round(st["p50_s"] * 1e3, 3), "p99_ms": round(st["p99_s"] * 1e3, 3),
+        "mean_ms": round(st["mean_s"] * 1e3, 3), "max_ms": round(st["max_s"] * 1e3, 3),
+        "span_s": round(span, 3), "arrival_span_s": round(offsets[-1], 3),
+        "effective_tflops": round(flops / span / 1e12, 2) if span == span else None,
+        "per_call_native": dict(base, sample=len(sample)),
+        "per_call_same_paths": dict(same, sample=len(sample)),
+        "speedup_vs_per_call": round(st["solves_per_s"] / base["solves_per_s"], 2),
+        "speedup_vs_per_call_same_paths": round(st["solves_per_s"] / same["solves_per_s"], 2),
+        "error": err, "clocks": clk,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def serve_errors(torch, eb, call, stream, built, per_kind=12, max_work=1 << 30):
+    """Componentwise error max |r - e| / (|alpha||A||B| + |beta||C|) of the
+    served paths (split-BF16, Ozaki) and of the native per-call kernels on
+    gemm requests of the stream (m n k <= max_work), against torch FP64
+    (FP32 requests) or against each other (FP64 requests)."""
+    out = {"fp32_split_max": 0.0, "fp32_native_max": 0.0, "fp64_ozaki_vs_native_max": 0.0, "checked": 0}
+    seen = {1: 0, 2: 0}
+    eb.set_blocking(True)
+    for (_, op, p, m, n, k), (r, views) in zip(stream, built):
+        if op != "gemm" or m * n * k > max_work or seen[p] >= per_kind:
+            continue
+        seen[p] += 1
+        A, B, Cm = views
+        C0 = Cm.clone()
+        A2, B2 = A.view(m, k).double(), B.view(k, n).double()
+        mag = (A2.abs() @ B2.abs()) * abs(r.alpha) + C0.view(m, n).double().abs() * abs(r.beta)
+        res = {}
+        for mode in (0, 1 if p == 1 else 2):
+            Cm.copy_(C0)
+            torch.cuda.synchronize()
+            eb.set_precision(mode)
+            call(r)
+            res[mode] = Cm.view(m, n).double().clone()
+        eb.set_precision(0)
+        Cm.copy_(C0)
+        torch.cuda.synchronize()
+        if p == 1:
+            ref = r.alpha * (A2 @ B2) + r.beta * C0.view(m, n).double()
+            out["fp32_native_max"] = max(out["fp32_native_max"], float(((res[0] - ref).abs() / mag).max()))
+            out["fp32_split_max"] = max(out["fp32_split_max"], float(((res[1] - ref).abs() / mag).max()))
+        else:
+            out["fp64_ozaki_vs_native_max"] = max(out["fp64_ozaki_vs_native_max"],
+                                                  float(((res[2] - res[0]).abs() / mag).max()))
+        out["checked"] += 1
+    eb.set_blocking(False)
+    return {k: (float(f"{v:.3e}") if isinstance(v, float) else v) for k, v in out.items()}
 
 
 def run_reference(args):

@@ -14,6 +14,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libexoblas_gb300.so"
 
 # C type codes used in the signature table
 _T = {
+    "z": C.c_size_t,
     "i": C.c_int,
     "f": C.c_float,
     "d": C.c_double,
@@ -93,6 +94,14 @@ EXTRA = {
     "exoblas_batch_plan_destroy": ("i", "p"),
     "exoblas_batch_tune": ("i", ""),
     "exoblas_batch_tile_config": ("i", "iii"),
+    "exoblas_server_create": ("i", "izzzp"),
+    "exoblas_server_submit": ("i", "ppd"),
+    "exoblas_server_now": ("d", ""),
+    "exoblas_server_replay": ("i", "pppzp"),
+    "exoblas_server_drain": ("i", "p"),
+    "exoblas_server_stats": ("i", "pp"),
+    "exoblas_server_destroy": ("i", "p"),
+    "exoblas_reserve_scratch": ("i", "z"),
 }
 
 SIGNATURES = {**L1, **L2, **L3, **EXTRA}

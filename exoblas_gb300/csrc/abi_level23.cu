@@ -58,6 +58,8 @@ static void symm_dispatch(bool left, bool upper, long m, long n, float alpha, co
 }
 static void symm_dispatch(bool left, bool upper, long m, long n, double alpha, const double *A, long lda,
                           const double *B, long ldb, double beta, double *C, long ldc) {
+  if (ctx().precision == EXOBLAS_PRECISION_OZAKI && l3::dsymm_ozaki(left, upper, m, n, alpha, A, lda, B, ldb, beta, C, ldc))
+    return;
   l3::symm_simt<double>(left, upper, m, n, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 static void syrk_dispatch(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
@@ -69,6 +71,9 @@ static void syrk_dispatch(bool upper, bool trans, long n, long k, float alpha, c
 }
 static void syrk_dispatch(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, double beta,
                           double *C, long ldc) {
+  if (ctx().precision == EXOBLAS_PRECISION_OZAKI && k > 0 &&
+      l3::dsyrk_ozaki(upper, trans, n, k, alpha, A, lda, beta, C, ldc))
+    return;
   l3::syrk_simt<double>(upper, trans, n, k, alpha, A, lda, beta, C, ldc);
 }
 

@@ -376,13 +376,12 @@ static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, floa
   p.C = C;
   p.ldc = ldc;
   p.status = device_status_word();
-  static bool attr[64] = {};
+  static std::once_flag attr[64];
   const int smem = kStages * kStageBytes + 1024;
   const int dev = c.device < 64 ? c.device : 63;
-  if (!attr[dev]) {
+  std::call_once(attr[dev], [smem] {
     EXB_CUDA(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr[dev] = true;
-  }
+  });
   const int grid = p.tiles < c.sm_count ? p.tiles : c.sm_count;
   split_bf16_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(ma, mb, p);
   EXB_LAUNCH("split-bf16 tcgen05 gemm kernel");

@@ -71,6 +71,10 @@ void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const 
 // (nothing written; the caller uses the FP64 FMA kernel)
 bool dgemm_ozaki(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda, const double *B,
                  long ldb, double beta, double *C, long ldc);
+bool dsymm_ozaki(bool left, bool upper, long m, long n, double alpha, const double *A, long lda, const double *B,
+                 long ldb, double beta, double *C, long ldc);
+bool dsyrk_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, double beta,
+                 double *C, long ldc);
 }  // namespace l3
 
 }  // namespace exb

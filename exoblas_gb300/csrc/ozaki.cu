@@ -28,6 +28,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "runtime.h"
@@ -60,6 +62,7 @@ struct Params {
   int M, N, K;
   int Mp, Np, kblocks;
   int mtiles, ntiles, tiles;
+  int tri;  // 0 full, 1 lower, 2 upper (syrk: only that triangle is written)
   double alpha, beta;
   double *C;
   long ldc;
@@ -67,6 +70,23 @@ struct Params {
   const int *fb;  // biased max exponent per column of op(B)
   int *status;
 };
+
+// tile index -> (mt, nt).  Triangle mode walks the 128 x 128 blocks on and
+// below (lower) or above (upper) the diagonal, two 64-wide n-tiles each.
+__device__ __forceinline__ void tile_mn(const Params &p, int t, int &mt, int &nt) {
+  if (!p.tri) {
+    mt = t % p.mtiles;
+    nt = t / p.mtiles;
+    return;
+  }
+  const int b = t >> 1;
+  int r = int((sqrtf(8.f * float(b) + 1.f) - 1.f) * 0.5f);
+  while (r * (r + 1) / 2 > b) --r;
+  while ((r + 1) * (r + 2) / 2 <= b) ++r;
+  const int c = b - r * (r + 1) / 2;
+  mt = p.tri == 1 ? r : c;
+  nt = 2 * (p.tri == 1 ? c : r) + (t & 1);
+}
 
 __global__ void __launch_bounds__(kThreads, 1)
     ozaki_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, Params p) {
@@ -101,7 +121,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t round = 0;
       long issued = 0;
       for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
-        const int mt = t % p.mtiles, nt = t / p.mtiles;
+        int mt, nt;
+        tile_mn(p, t, mt, nt);
         for (int kb = 0; kb < p.kblocks; ++kb) {
           if (!mbar_wait(&empty[stage], (round & 1) ^ 1, &abort_flag, p.status)) break;
           mbar_expect_tx(&full[stage], kStageBytes);
@@ -175,7 +196,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int row = q * 32 + lane;
     uint32_t chunk = 0;
     for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
-      const int mt = t % p.mtiles, nt = t / p.mtiles;
+      int mt, nt;
+      tile_mn(p, t, mt, nt);
       long long H[kEpiCols], L[kEpiCols];
 #pragma unroll
       for (int j = 0; j < kEpiCols; ++j) H[j] = L[j] = 0;
@@ -214,7 +236,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int j = 0; j < kEpiCols; ++j) {
           const long gj = gj0 + j;
-          if (gj < p.N) {
+          if (gj < p.N && !(p.tri == 1 && gj > gi) && !(p.tri == 2 && gj < gi)) {
             const int fj = p.fb[gj] - 1022;
             const double v = scalbn(fma(double(H[j]), 268435456.0, double(L[j])), ei + fj - 63);
             crow[gj] = p.alpha * v + p.beta * crow[gj];
@@ -235,9 +257,16 @@ __global__ void __launch_bounds__(kThreads, 1)
 struct View {  // X(r, k) of the logical rows x K operand
   const double *p;
   long ld;
-  bool t;  // element (r, k) at p[k * ld + r]
-  __device__ double operator()(int r, int k) const { return t ? p[long(k) * ld + r] : p[long(r) * ld + k]; }
-  __device__ bool k_contiguous() const { return !t; }
+  bool t;       // element (r, k) at p[k * ld + r]
+  int sym = 0;  // 1 / 2: symmetric, only the upper / lower triangle stored
+  __device__ double operator()(int r, int k) const {
+    if (sym) {
+      const bool direct = sym == 1 ? r <= k : r >= k;
+      return direct ? p[long(r) * ld + k] : p[long(k) * ld + r];
+    }
+    return t ? p[long(k) * ld + r] : p[long(r) * ld + k];
+  }
+  __device__ bool k_contiguous() const { return sym || !t; }
 };
 
 __device__ __forceinline__ int biased_exp(double x) {
@@ -334,9 +363,9 @@ __global__ void ozaki_slice_kernel(View X, int rows, int K, int Rp, int Kp, cons
 static int round_up(long v, int m) { return int((v + m - 1) / m * m); }
 
 static void init_products() {
-  static bool done[64] = {};
+  static std::once_flag once[64];
   const int dev = ctx().device < 64 ? ctx().device : 63;
-  if (done[dev]) return;
+  std::call_once(once[dev], [] {
   signed char ps[kProducts], pt[kProducts];
   int q = 0;
   for (int d = 0; d < kS; ++d)
@@ -347,39 +376,44 @@ static void init_products() {
     }
   EXB_CUDA(cudaMemcpyToSymbol(kPs, ps, sizeof ps));
   EXB_CUDA(cudaMemcpyToSymbol(kPt, pt, sizeof pt));
-  done[dev] = true;
+  });
 }
 
 // Returns false (nothing written) when an input holds NaN or infinity; the
 // caller then uses the FP64 FMA kernel, which propagates them.
-bool dgemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, long lda, const double *B, long ldb,
-           double beta, double *C, long ldc) {
+// C[M, N] = alpha X_A X_B^T + beta C with X_A (M x K) and X_B (N x K).
+// tri != 0 (syrk): X_B is X_A, N == M, only that triangle of C is written;
+// the operand is scaled and sliced once.
+static bool run(const View &xa, const View &xb, int M, int N, int K, double alpha, double beta, double *C, long ldc,
+                int tri) {
   Context &c = ctx();
   init_products();
-  const int Kp = round_up(K, BK * kChunkKB), Mp = round_up(M, BM), Np = round_up(N, BN);
-  const size_t a_elems = size_t(kS) * Mp * Kp, b_elems = size_t(kS) * Np * Kp;
+  const bool same_ab = tri != 0;
+  const int Kp = round_up(K, BK * kChunkKB), Mp = round_up(M, BM), Np = tri ? Mp : round_up(N, BN);
+  const size_t a_elems = size_t(kS) * Mp * Kp, b_elems = same_ab ? 0 : size_t(kS) * Np * Kp;
   const size_t ebytes = (size_t(Mp + Np + 64) * 4 + 255) & ~size_t(255);
   char *ws = static_cast<char *>(scratch((a_elems + b_elems) * 2 + ebytes + 512));
   __nv_bfloat16 *sa = reinterpret_cast<__nv_bfloat16 *>(ws);
-  __nv_bfloat16 *sb = sa + a_elems;
+  __nv_bfloat16 *sb = same_ab ? sa : sa + a_elems;
   int *ea = reinterpret_cast<int *>(ws + (a_elems + b_elems) * 2);
-  int *fb = ea + Mp;
-  int *bad = fb + Np;
+  int *fb = same_ab ? ea : ea + Mp;
+  int *bad = ea + Mp + Np;
   EXB_CUDA(cudaMemsetAsync(ea, 0, ebytes, c.stream));
-  const View xa{A, lda, ta};
-  const View xb{B, ldb, !tb};  // X_B(j, k) = op(B)[k][j]
   ozaki_exp_kernel<<<dim3(unsigned(ceil_div(K, 32)), unsigned(ceil_div(M, 32))), 256, 0, c.stream>>>(xa, M, K, ea, bad);
-  ozaki_exp_kernel<<<dim3(unsigned(ceil_div(K, 32)), unsigned(ceil_div(N, 32))), 256, 0, c.stream>>>(xb, N, K, fb, bad);
+  if (!same_ab)
+    ozaki_exp_kernel<<<dim3(unsigned(ceil_div(K, 32)), unsigned(ceil_div(N, 32))), 256, 0, c.stream>>>(xb, N, K, fb,
+                                                                                                        bad);
   EXB_LAUNCH("ozaki exponent kernel");
-  count_launch(2);
+  count_launch(same_ab ? 1 : 2);
   int hbad = 0;
   EXB_CUDA(cudaMemcpyAsync(&hbad, bad, 4, cudaMemcpyDeviceToHost, c.stream));
   EXB_CUDA(cudaStreamSynchronize(c.stream));
   if (hbad) return false;
   ozaki_slice_kernel<<<dim3(unsigned(Kp / 32), unsigned(Mp / 32)), 256, 0, c.stream>>>(xa, M, K, Mp, Kp, ea, sa);
-  ozaki_slice_kernel<<<dim3(unsigned(Kp / 32), unsigned(Np / 32)), 256, 0, c.stream>>>(xb, N, K, Np, Kp, fb, sb);
+  if (!same_ab)
+    ozaki_slice_kernel<<<dim3(unsigned(Kp / 32), unsigned(Np / 32)), 256, 0, c.stream>>>(xb, N, K, Np, Kp, fb, sb);
   EXB_LAUNCH("ozaki slice kernel");
-  count_launch(2);
+  count_launch(same_ab ? 1 : 2);
   const CUtensorMap ma = make_map(sa, long(kS) * Mp, Kp, BK, BM);
   const CUtensorMap mb = make_map(sb, long(kS) * Np, Kp, BK, BN);
   Params p;
@@ -391,7 +425,8 @@ bool dgemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A,
   p.kblocks = Kp / BK;
   p.mtiles = Mp / BM;
   p.ntiles = Np / BN;
-  p.tiles = p.mtiles * p.ntiles;
+  p.tri = tri;
+  p.tiles = tri ? p.mtiles * (p.mtiles + 1) : p.mtiles * p.ntiles;
   p.alpha = alpha;
   p.beta = beta;
   p.C = C;
@@ -399,13 +434,12 @@ bool dgemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A,
   p.ea = ea;
   p.fb = fb;
   p.status = device_status_word();
-  static bool attr[64] = {};
+  static std::once_flag attr[64];
   const int smem = kStages * kStageBytes + 1024;
   const int dev = c.device < 64 ? c.device : 63;
-  if (!attr[dev]) {
+  std::call_once(attr[dev], [smem] {
     EXB_CUDA(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr[dev] = true;
-  }
+  });
   const int grid = p.tiles < c.sm_count ? p.tiles : c.sm_count;
   ozaki_gemm_kernel<<<grid, kThreads, smem, c.stream>>>(ma, mb, p);
   EXB_LAUNCH("ozaki tcgen05 gemm kernel");
@@ -419,7 +453,27 @@ bool dgemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A,
 bool dgemm_ozaki(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda, const double *B,
                  long ldb, double beta, double *C, long ldc) {
   if (m <= 0 || n <= 0 || k <= 0) return false;
-  return oz::dgemm(ta, tb, int(m), int(n), int(k), alpha, A, lda, B, ldb, beta, C, ldc);
+  // X_A = op(A); X_B(j, k) = op(B)[k][j]
+  return oz::run(oz::View{A, lda, ta}, oz::View{B, ldb, !tb}, int(m), int(n), int(k), alpha, beta, C, ldc, 0);
+}
+
+// C_tri = alpha op(A) op(A)^T + beta C_tri over the stored triangle only
+// (syrk; op(A) = A for NoTrans, A^T for Trans).
+bool dsyrk_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, double beta,
+                 double *C, long ldc) {
+  if (n <= 0 || k <= 0) return false;
+  const oz::View x{A, lda, trans};
+  return oz::run(x, x, int(n), int(n), int(k), alpha, beta, C, ldc, upper ? 2 : 1);
+}
+
+// C = alpha sym(A) B + beta C (left) or alpha B sym(A) + beta C (right),
+// sym(A) read from its stored triangle.
+bool dsymm_ozaki(bool left, bool upper, long m, long n, double alpha, const double *A, long lda, const double *B,
+                 long ldb, double beta, double *C, long ldc) {
+  if (m <= 0 || n <= 0) return false;
+  const oz::View sa{A, lda, false, upper ? 1 : 2};
+  if (left) return oz::run(sa, oz::View{B, ldb, true}, int(m), int(n), int(m), alpha, beta, C, ldc, 0);
+  return oz::run(oz::View{B, ldb, false}, sa, int(m), int(n), int(n), alpha, beta, C, ldc, 0);
 }
 
 }  // namespace l3

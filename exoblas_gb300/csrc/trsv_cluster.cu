@@ -33,6 +33,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "runtime.h"
@@ -515,6 +517,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   // cluster size: 16 where two or more such clusters fit, else 8 (cached per device)
   static int cs_cache[64] = {0};
   static int mc_cache[64] = {0};
+  static std::once_flag probed[64];
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -526,7 +529,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   const int dev = c.device < 64 ? c.device : 63;
-  if (cs_cache[dev] == 0) {
+  std::call_once(probed[dev], [&] {
     const int m16 = max_clusters<T, 16>(cfg, attr);
     const int m8 = max_clusters<T, 8>(cfg, attr);
     if (m16 >= 4) {
@@ -536,7 +539,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
       cs_cache[dev] = 8;
       mc_cache[dev] = m8;
     }
-  }
+  });
   const int CS = cs_cache[dev];
   const long maxc = mc_cache[dev];
   if (maxc < 1) return false;

@@ -25,6 +25,8 @@
 #ifndef EXOBLAS_GB300_H
 #define EXOBLAS_GB300_H
 
+#include <stddef.h>
+
 #if defined(__GNUC__)
 #define EXOBLAS_API __attribute__((visibility("default")))
 #else
@@ -83,13 +85,15 @@ EXOBLAS_API int exoblas_set_blocking(int blocking);
  * kernel queued in non-blocking mode (trsv) gave up a bounded wait. */
 EXOBLAS_API int exoblas_synchronize(void);
 
-/* Arithmetic used by exo_sgemm/ssymm/ssyrk and exo_dgemm:
+/* Arithmetic used by exo_sgemm/ssymm/ssyrk and exo_dgemm/dsymm/dsyrk:
  *   EXOBLAS_PRECISION_NATIVE    FP32 FFMA / FP64 DFMA kernels (default)
  *   EXOBLAS_PRECISION_SPLIT_BF16 sgemm/ssymm/ssyrk: each FP32 operand split
  *                               into three BF16 terms, products on tcgen05
  *                               tensor cores, FP32 accumulation
- *   EXOBLAS_PRECISION_OZAKI     dgemm: Ozaki slice emulation with exact
- *                               integer accumulation of small-integer slices
+ *   EXOBLAS_PRECISION_OZAKI     dgemm/dsymm/dsyrk: Ozaki slice emulation
+ *                               with exact integer accumulation of
+ *                               small-integer slices (inputs holding NaN or
+ *                               infinity take the DFMA kernels)
  * The environment variable EXOBLAS_PRECISION_MODE (native | split_bf16 |
  * ozaki) sets the initial value for every thread. */
 enum EXOBLAS_PRECISION { EXOBLAS_PRECISION_NATIVE = 0, EXOBLAS_PRECISION_SPLIT_BF16 = 1, EXOBLAS_PRECISION_OZAKI = 2 };
@@ -257,6 +261,56 @@ EXOBLAS_API int exoblas_batch_plan_destroy(exoblas_batch_plan plan);
 EXOBLAS_API int exoblas_batch_tune(void);
 /* tile configuration the autotuner picked for an sgemm of this shape (0: 32x32, 1: 64x64, 2: 128x128) */
 EXOBLAS_API int exoblas_batch_tile_config(int m, int n, int k);
+
+/* ------------------------------------------------------------- serving --- */
+/* A request server with continuous batching (no counterpart in the
+ * reference).  W worker threads, each with its own stream and workspace,
+ * take requests as they arrive; a request is admitted when a worker is free
+ * and its estimated device-memory footprint fits in the admission budget
+ * with everything in flight, so requests arriving while others run start as
+ * soon as a slot and memory free up and their work overlaps on the device.
+ * Operands are device pointers.  Single-precision gemm / syrk run the
+ * split-BF16 path, double gemm / syrk the Ozaki path, gemv / trsv their
+ * kernels.
+ *   GEMM: flags = {TransA, TransB}, m, n, k, A/lda, B/ldb, C/ldc
+ *   SYRK: flags = {Uplo, Trans}, m = N, k = K, A/lda, C/ldc
+ *   GEMV: flags = {TransA}, m = M, n = N, A/lda, B = X (ldb = incX), C = Y (ldc = incY)
+ *   TRSV: flags = {Uplo, TransA, Diag}, m = N, A/lda, C = X (ldc = incX)
+ * precision: 1 single, 2 double.  Arrivals beyond the queue capacity are
+ * rejected and counted. */
+enum EXOBLAS_REQUEST_OP { EXOBLAS_REQ_GEMM = 1, EXOBLAS_REQ_GEMV = 2, EXOBLAS_REQ_TRSV = 3, EXOBLAS_REQ_SYRK = 4 };
+typedef struct exoblas_request {
+  int op;
+  int precision;
+  int flags[3];
+  int m, n, k;
+  double alpha, beta;
+  const void *A;
+  int lda;
+  const void *B;
+  int ldb;
+  void *C;
+  int ldc;
+} exoblas_request;
+typedef struct exoblas_server_s *exoblas_server;
+/* hbm_budget_bytes = 0: 70% of the free device memory; queue_capacity = 0:
+ * unbounded; scratch_reserve_bytes: workspace each worker allocates up front */
+EXOBLAS_API int exoblas_server_create(int workers, size_t hbm_budget_bytes, size_t queue_capacity,
+                                      size_t scratch_reserve_bytes, exoblas_server *server);
+/* arrival_s on the exoblas_server_now() clock (< 0: now) */
+EXOBLAS_API int exoblas_server_submit(exoblas_server server, const exoblas_request *request, double arrival_s);
+EXOBLAS_API double exoblas_server_now(void);
+/* submits requests[i] at t0 + offsets_s[i], t0 = the call's start (written
+ * to *t0_out when not NULL); returns once the last one is submitted */
+EXOBLAS_API int exoblas_server_replay(exoblas_server server, const exoblas_request *requests, const double *offsets_s,
+                                      size_t count, double *t0_out);
+EXOBLAS_API int exoblas_server_drain(exoblas_server server);
+/* stats[0..7]: completed, rejected, failed, p50 latency s, p99 s, mean s,
+ * max s, completed per second (first arrival to last completion) */
+EXOBLAS_API int exoblas_server_stats(exoblas_server server, double *stats);
+EXOBLAS_API int exoblas_server_destroy(exoblas_server server);
+/* grows the calling thread's device workspace to at least `bytes` now */
+EXOBLAS_API int exoblas_reserve_scratch(size_t bytes);
 
 #ifdef __cplusplus
 }

@@ -1,4 +1,4 @@
-"""Ozaki slice emulation of dgemm on tcgen05 tensor cores.
+"""Ozaki slice emulation of dgemm / dsymm / dsyrk on tcgen05 tensor cores.
 
 Results must meet the FP64 componentwise bound against the double-double
 oracle (the reference grid of test/level3/gemm/correctness.cpp in double,
@@ -8,7 +8,7 @@ propagate as in the reference)."""
 import numpy as np
 import pytest
 
-from cases import gemm_cases
+from cases import gemm_cases, symm_cases, syrk_cases
 from common import EPS, check_case, run_gpu
 
 
@@ -21,7 +21,9 @@ def ozaki_mode(cuda):
     eb.set_precision(eb.PRECISION_NATIVE)
 
 
-CASES = [c for c in gemm_cases("d", dims=(1, 7, 64, 257), ldds=(0, 5))][::3]
+CASES = ([c for c in gemm_cases("d", dims=(1, 7, 64, 257), ldds=(0, 5))][::3]
+         + [c for c in symm_cases("d", dims=(1, 7, 64, 257))][::2]
+         + [c for c in syrk_cases("d", dims=(1, 7, 64, 257, 300))][::2])
 
 
 @pytest.mark.gpu
