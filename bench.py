@@ -77,6 +77,7 @@ def parse():
     ap.add_argument("--workers", type=int, default=8, help="serve: server worker streams")
     ap.add_argument("--per-call-sample", type=int, default=2000, help="serve: requests timed per call")
     ap.add_argument("--size", type=int, default=8192, help="M = N = K of the precision set")
+    ap.add_argument("--kernels", default="", help="bandwidth: comma list, a subset of the set (profiling runs)")
     return ap.parse_args()
 
 
@@ -148,26 +149,28 @@ class Clocks:
 
 
 # ------------------------------------------------------------- workloads --
-def make_inputs(torch, dev):
+def make_inputs(torch, dev, names=None):
     g = torch.Generator(device=dev).manual_seed(0)
 
     def u(n, dt):
         return (torch.rand(n, generator=g, device=dev, dtype=dt) * 2 - 1)
 
     f, d = torch.float32, torch.float64
-    X = {
-        "saxpy": (u(N1S, f), u(N1S, f)),
-        "sdot": (u(N1S, f), u(N1S, f)),
-        "dsdot": (u(N1S, f), u(N1S, f)),
-        "daxpy": (u(N1D, d), u(N1D, d)),
-        "ddot": (u(N1D, d), u(N1D, d)),
-        "sgemv_n": (u(NG * NG, f), u(NG, f), u(NG, f)),
-        "sgemv_t": (u(NG * NG, f), u(NG, f), u(NG, f)),
+    make = {
+        "saxpy": lambda: (u(N1S, f), u(N1S, f)),
+        "sdot": lambda: (u(N1S, f), u(N1S, f)),
+        "dsdot": lambda: (u(N1S, f), u(N1S, f)),
+        "daxpy": lambda: (u(N1D, d), u(N1D, d)),
+        "ddot": lambda: (u(N1D, d), u(N1D, d)),
+        "sgemv_n": lambda: (u(NG * NG, f), u(NG, f), u(NG, f)),
+        "sgemv_t": lambda: (u(NG * NG, f), u(NG, f), u(NG, f)),
     }
-    A = torch.rand(NT, NT, generator=g, device=dev, dtype=d).mul_(2).sub_(1).div_(NT)
-    idx = torch.arange(NT, device=dev)
-    A[idx, idx] = 1.0 + torch.rand(NT, generator=g, device=dev, dtype=d)
-    X["dtrsv"] = (A.reshape(-1), u(NT, d))
+    X = {k: make[k]() for k in (names or BYTES) if k in make}
+    if "dtrsv" in (names or BYTES):
+        A = torch.rand(NT, NT, generator=g, device=dev, dtype=d).mul_(2).sub_(1).div_(NT)
+        idx = torch.arange(NT, device=dev)
+        A[idx, idx] = 1.0 + torch.rand(NT, generator=g, device=dev, dtype=d)
+        X["dtrsv"] = (A.reshape(-1), u(NT, d))
     return X
 
 
@@ -323,11 +326,15 @@ def main():
     eb.set_stream(stream)
     eb.set_blocking(False)
 
-    X = make_inputs(torch, f"cuda:{local}")
+    names = [k for k, _ in KERNELS]
+    if args.kernels:
+        names = [k for k in names if k in args.kernels.split(",")]
+        if not names:
+            raise SystemExit(f"--kernels: none of {args.kernels!r} in {[k for k, _ in KERNELS]}")
+    X = make_inputs(torch, f"cuda:{local}", names)
     res = torch.zeros(8, dtype=torch.float64, device=f"cuda:{local}")
     torch.cuda.synchronize()  # inputs were generated on the default stream
     run = launchers(L, X, res)
-    names = [k for k, _ in KERNELS]
 
     def step(evs=None):
         for i, k in enumerate(names):
@@ -373,7 +380,7 @@ def main():
         dist.barrier()
 
     per = {k: statistics.mean(evs[s][i][0].elapsed_time(evs[s][i][1]) for s in range(K)) for i, k in enumerate(names)}
-    step_bytes = sum(BYTES.values())
+    step_bytes = sum(BYTES[k] for k in names)
     ms_per_step = total_ms / K
     value = world * step_bytes / (ms_per_step * 1e-3) / 1e9
 
