@@ -60,9 +60,12 @@ static void launch_rowdot(long rows, long cols, T alpha, const T *A, long lda, c
   const bool vec = vec_ok(A, lda) && aligned16(xu);
   const int G = cols >= 256 ? 32 : 4;
   const long rpb = (kThreads / 32) * (32 / G);
-  long blocks = ceil_div(rows, rpb);
-  if (blocks > grid_cap(16)) blocks = grid_cap(16);
-  if (blocks < 1) blocks = 1;
+  // whole waves of equal row counts per warp (no partial last wave)
+  const void *kern = G == 32 ? (vec ? reinterpret_cast<const void *>(rowdot_kernel<T, 32, true, MODE>)
+                                    : reinterpret_cast<const void *>(rowdot_kernel<T, 32, false, MODE>))
+                             : (vec ? reinterpret_cast<const void *>(rowdot_kernel<T, 4, true, MODE>)
+                                    : reinterpret_cast<const void *>(rowdot_kernel<T, 4, false, MODE>));
+  const long blocks = balanced_grid(ceil_div(rows, rpb), kern, kThreads);
 #define EXB_ROWDOT(GG, VV) \
   rowdot_kernel<T, GG, VV, MODE><<<int(blocks), kThreads, 0, s>>>(rows, cols, alpha, A, lda, xu, beta, y, incy, tri, unit)
   if (G == 32) {

@@ -6,7 +6,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 
 #include "common.cuh"
 #include "runtime.h"
@@ -309,3 +312,31 @@ void exoblas_staged_bytes(unsigned long long *h2d, unsigned long long *d2h) {
 }
 
 }  // extern "C"
+
+namespace exb {
+
+int resident_per_sm(const void *kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, int> cache;
+  const int dev = ctx().device;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({dev, kernel});
+    if (it != cache.end()) return it->second;
+  }
+  int per_sm = 0;
+  EXB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[{dev, kernel}] = per_sm;
+  return per_sm;
+}
+
+long balanced_grid(long want, const void *kernel, int threads, size_t smem) {
+  if (want < 1) return 1;
+  const long wave = long(ctx().sm_count) * resident_per_sm(kernel, threads, smem);
+  const long waves = ceil_div(want, wave);
+  return ceil_div(want, waves);
+}
+
+}  // namespace exb

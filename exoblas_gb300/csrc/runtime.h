@@ -10,6 +10,14 @@
 namespace exb {
 
 void count_launch(unsigned n = 1);
+// CTAs of `kernel` (threads per CTA, dynamic shared memory) resident at once
+// on one SM of the current device; cached per device and kernel.
+int resident_per_sm(const void *kernel, int threads, size_t smem = 0);
+// a grid of at most `want` CTAs that runs in whole waves of equal work:
+// want is split into the fewest waves of the device's resident CTAs and the
+// grid is the per-wave share, so every CTA of a grid-stride loop gets the
+// same number of items
+long balanced_grid(long want, const void *kernel, int threads, size_t smem = 0);
 bool is_device_pointer(const void *p);
 void set_status(int s);
 void report(int status, const char *fn, const char *msg);

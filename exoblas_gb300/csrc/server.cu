@@ -184,7 +184,7 @@ int exoblas_server_create(int workers, size_t hbm_budget_bytes, size_t queue_cap
     EXB_CUDA(cudaMemGetInfo(&freeb, &total));
     const size_t auto_budget = freeb / 10 * 7;
     s->budget = hbm_budget_bytes ? std::min(hbm_budget_bytes, auto_budget) : auto_budget;
-    s->queue_cap = queue_capacity ? queue_capacity : 1 << 20;
+    s->queue_cap = queue_capacity ? queue_capacity : ~size_t(0);
     s->scratch_reserve = scratch_reserve_bytes;
     for (int w = 0; w < workers; ++w) s->threads.emplace_back([s, w] { s->run_worker(w); });
     *out = reinterpret_cast<exoblas_server>(s);
