@@ -74,6 +74,7 @@ struct Args {
   int *status;
   int nb, nch;
   bool rev, trans, unit;
+  bool vec16;  // rows of L are contiguous, 16-byte aligned runs of A (lower no-trans, even lda)
 };
 
 __device__ __forceinline__ int ld_acquire(const int *p) {
@@ -402,6 +403,293 @@ __device__ void solve_chain(const Args<T> &a, SmemSolver<T, CS> &S, bool &dead) 
   cp_wait<0>();
 }
 
+// ------------------------------------------------- solver, 16-CTA form ----
+// Warps 0..3 of each solver CTA are the critical warps (warp w owns row
+// R*4+w of every block), warps 4..7 the helpers.  The two exchanges of a
+// step are asynchronous remote shared-memory stores (st.async) that count
+// their bytes against an mbarrier in the receiving CTA (armed once per phase
+// with the 64 values it expects), so only the critical warps take part in
+// them, no sender waits for its stores, and no step waits on a cluster
+// barrier.
+// The helpers prepare step K+1 meanwhile (operand prefetch, the near tiles
+// L[K+1, K-1..K-5] x, the bulk slot sums, publishing x to global memory)
+// and hand the carry over through a local mbarrier.
+//
+// Barrier rings and why their parities cannot alias: E1 (residuals, ring 2)
+// phase K completes only when every critical warp sent its step-K residual,
+// which it does after waiting for phase K-2 of the same barrier.  Critical
+// warp 0 re-arms a barrier for its next phase right after observing a phase
+// complete; data of that next phase cannot land earlier, and if it did the
+// phase would still wait for the arming arrival.  E2 (x,
+// ring 4) phase m+4 needs the step-(m+4) residuals, which need the carries
+// of step m+4, which the helpers produce after their last wait on phase m.
+// The carry barrier (ring 2) phase K+2 is armed by the helpers only after
+// E2 phase K, i.e. after the critical warps consumed phase K.
+constexpr int kCS2 = 16;
+constexpr int kRPC2 = kTB / kCS2;  // 4
+constexpr long long kWaitCycles = 4ll << 30;
+
+template <typename T>
+struct SmemSolver2 {
+  static constexpr int kStage = (kD + 1) * kRPC2 * kTB;  // near tiles j = 0..kD-1, then inv rows
+  T stage[kPre][kStage];
+  T bvals[kPre][kRPC2];
+  T rfull[2][kTB];
+  T xring[kXR][kTB];
+  T carry[2][kRPC2];
+  unsigned long long e1bar[2];
+  unsigned long long e2bar[4];
+  unsigned long long cready[2];
+};
+
+__device__ __forceinline__ uint32_t sh_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint32_t map_rank(uint32_t a, int rank) {
+  uint32_t o;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(o) : "r"(a), "r"(rank));
+  return o;
+}
+// Remote store that completes `bytes` of the remote mbarrier's transaction
+// count when it lands (no fence on the sending thread).
+__device__ __forceinline__ void st_async(uint32_t a, double v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(a),
+               "l"(__double_as_longlong(v)), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t a, float v, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(a),
+               "r"(__float_as_uint(v)), "r"(bar)
+               : "memory");
+}
+// One local arrival that also expects `bytes` of remote stores this phase.
+__device__ __forceinline__ void arm(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sh_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void arrive_local(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void bar_init(uint32_t bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of parity `parity`, by a whole warp (the
+// outcome is warp-uniform); on expiry records the timeout and stops waiting
+// for the rest of the launch.
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, int *status, bool &dead) {
+  if (dead) return false;
+  const long long t0 = clock64();
+  for (;;) {
+    if (__all_sync(0xffffffffu, bar_try(bar, parity))) return true;
+    if (__shfl_sync(0xffffffffu, int(clock64() - t0 > kWaitCycles), 0)) {
+      if ((threadIdx.x & 31) == 0) atomicExch(status, 1);
+      dead = true;
+      return false;
+    }
+  }
+}
+__device__ __forceinline__ void helper_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+template <typename T>
+__device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
+  constexpr int RPC = kRPC2, CS = kCS2;
+  constexpr int kStage = SmemSolver2<T>::kStage;
+  cg::cluster_group cl = cg::this_cluster();
+  const int R = int(cl.block_rank());
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long n = a.n;
+  const int nb = a.nb;
+  constexpr uint32_t kXBytes = kTB * sizeof(T);  // one exchange: 64 values from the cluster
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) bar_init(sh_u32(&S.e1bar[i]), 1);
+    for (int i = 0; i < 4; ++i) bar_init(sh_u32(&S.e2bar[i]), 1);
+    for (int i = 0; i < 2; ++i) bar_init(sh_u32(&S.cready[i]), 4);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int i = 0; i < 2; ++i) arm(sh_u32(&S.e1bar[i]), kXBytes);
+    for (int i = 0; i < 4; ++i) arm(sh_u32(&S.e2bar[i]), kXBytes);
+  }
+  cl.sync();  // every barrier of the cluster is initialised before any remote arrive
+
+  // 64-entry row . v by one warp (FP64: one row per warp keeps the chains short)
+  auto rowdot = [&](const T *row, const T *v) -> T {
+    T s = fma(row[lane + 32], v[lane + 32], row[lane] * v[lane]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+  };
+
+  if (warp < RPC) {
+    // ---------------- critical warp: row R*RPC + w of every block
+    const int w = warp;
+    for (long K = 0; K < nb; ++K) {
+      bar_wait(sh_u32(&S.cready[K & 1]), uint32_t((K >> 1) & 1), a.status, dead);
+      const T *st = S.stage[K % kPre];
+      T t0 = T(0);
+      if (K >= 1) {
+        bar_wait(sh_u32(&S.e2bar[(K - 1) & 3]), uint32_t(((K - 1) >> 2) & 1), a.status, dead);
+        if (w == 0 && lane == 0) arm(sh_u32(&S.e2bar[(K - 1) & 3]), kXBytes);  // for step K+3
+        t0 = rowdot(st + w * kTB, S.xring[(K - 1) % kXR]);
+      }
+      const T rr = S.bvals[K % kPre][w] - S.carry[K & 1][w] - t0;
+      if (lane < CS)  // lane d hands the residual to CTA d
+        st_async(map_rank(sh_u32(&S.rfull[K & 1][R * RPC + w]), lane), rr, map_rank(sh_u32(&S.e1bar[K & 1]), lane));
+      bar_wait(sh_u32(&S.e1bar[K & 1]), uint32_t((K >> 1) & 1), a.status, dead);
+      if (w == 0 && lane == 0) arm(sh_u32(&S.e1bar[K & 1]), kXBytes);  // for step K+2
+      const T xk = rowdot(st + (kD * RPC + w) * kTB, S.rfull[K & 1]);
+      if (lane < CS)
+        st_async(map_rank(sh_u32(&S.xring[K % kXR][R * RPC + w]), lane), xk, map_rank(sh_u32(&S.e2bar[K & 3]), lane));
+    }
+  } else {
+    // ---------------- helper warps: warp RPC + h prepares row h's carry
+    const int h = warp - RPC;
+    const int ht = tid - RPC * 32;  // 0 .. 127
+    auto prefetch = [&](long K) {
+      if (K < nb && a.vec16) {
+        // helper warp h copies row h of each near tile and of the inverse,
+        // 16 bytes per lane
+        constexpr int kPer = 16 / int(sizeof(T)), kChunks = kTB / kPer;
+        T *st = S.stage[K % kPre];
+        const long gi = K * kTB + R * RPC + h;
+        if (lane < kChunks) {
+          for (int which = 0; which <= kD; ++which) {
+            T *dst = st + (which * RPC + h) * kTB + lane * kPer;
+            if (which == kD) {
+              cp_async16(dst, a.inv + (K * kTB + R * RPC + h) * kTB + lane * kPer);
+            } else {
+              const long J = K - 1 - which;
+              if (J >= 0 && gi < n)
+                cp_async16(dst, a.A + gi * a.lda + J * kTB + lane * kPer);
+              else
+                *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+            }
+          }
+        }
+      } else if (K < nb) {
+        T *st = S.stage[K % kPre];
+        for (int e = ht; e < kStage; e += 32 * (kNT / 32 - RPC)) {
+          const int which = e / (RPC * kTB), rem = e % (RPC * kTB);
+          const int r = rem / kTB, cc = rem % kTB;
+          const long gi = K * kTB + R * RPC + r;
+          if (which < kD) {
+            const long J = K - 1 - which;
+            const long gj = J * kTB + cc;
+            if (J >= 0 && gi < n && gj < n)
+              cp_async(st + e, a.A + lidx(a, gi, gj));
+            else
+              st[e] = T(0);
+          } else {
+            cp_async(st + e, a.inv + (K * kTB + R * RPC + r) * kTB + cc);
+          }
+        }
+      }
+      if (K < nb && ht < RPC) {
+        const long gi = K * kTB + R * RPC + ht;
+        if (gi < n)
+          cp_async(&S.bvals[K % kPre][ht], a.z + zidx(a, gi));
+        else
+          S.bvals[K % kPre][ht] = T(0);
+      }
+      cp_commit();
+    };
+    // x_m to global memory and its flag (one warp; the publishing CTA rotates)
+    auto publish = [&](long m) {
+      for (int t = lane; t < kTB; t += 32) {
+        const long gi = m * kTB + t;
+        if (gi < n) a.z[zidx(a, gi)] = S.xring[m % kXR][t];
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release(a.xflag + m, 1);
+    };
+    for (int p = 0; p < kPre; ++p) prefetch(p);
+    cp_wait<kPre - 1>();
+    helper_sync();
+    if (lane == 0) {
+      S.carry[0][h] = T(0);
+      arrive_local(sh_u32(&S.cready[0]));
+    }
+    // bulk slots of the row being prepared, loaded one iteration ahead so
+    // the loads are in flight while other work runs (lane c: slots c, c + 32)
+    T p0 = T(0), p1 = T(0), pmore = T(0);
+    // Iteration T1 prepares the carry of step T1.  It starts when x_{T1-2}
+    // is exchanged: the stage of step T1-2 is then free for step T1-2+kPre
+    // and x_{T1-2} can be published; the carry (near tiles up to x_{T1-2}
+    // and the bulk slots) follows at once, the poll for the next row's bulk
+    // slots last.
+    for (long T1 = 1; T1 < nb; ++T1) {
+      if (T1 >= 2) {
+        bar_wait(sh_u32(&S.e2bar[(T1 - 2) & 3]), uint32_t(((T1 - 2) >> 2) & 1), a.status, dead);
+        prefetch(T1 - 2 + kPre);
+        if (h == RPC - 1 && (T1 - 2) % CS == R) publish(T1 - 2);
+      } else {
+        cp_commit();  // one group per iteration
+      }
+      // groups so far: stages 0..kPre-1, one empty, then stage g-1 in group
+      // g; stage T1 is complete once at most two groups are outstanding
+      cp_wait<kPre - 2>();
+      helper_sync();
+      const T *st = S.stage[T1 % kPre];
+      T s0 = T(0), s1 = T(0);
+      for (int j = 1; j < kD; ++j) {
+        const long J = T1 - 1 - j;
+        if (J < 0) break;
+        const T *row = st + (j * RPC + h) * kTB;
+        const T *xv = S.xring[J % kXR];
+        s0 = fma(row[lane], xv[lane], s0);
+        s1 = fma(row[lane + 32], xv[lane + 32], s1);
+      }
+      T sum = (s0 + s1) + ((p0 + p1) + pmore);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) {
+        S.carry[T1 & 1][h] = sum;
+        arrive_local(sh_u32(&S.cready[T1 & 1]));
+      }
+      // bulk slots of row T1 + 1, added in the next iteration
+      p0 = p1 = pmore = T(0);
+      const long K2 = T1 + 1;
+      const int nc = K2 < nb ? nch_row(K2) : 0;
+      if (nc > 0 && !dead) {
+        const long long t0 = clock64();
+        for (;;) {
+          int ok = 1;
+          for (int cc = lane; cc < nc; cc += 32) ok &= ld_acquire(a.sflag + K2 * a.nch + cc) != 0;
+          if (__all_sync(0xffffffffu, ok)) break;
+          if (__shfl_sync(0xffffffffu, int(clock64() - t0 > kWaitCycles), 0)) {
+            if (lane == 0) atomicExch(a.status, 1);
+            dead = true;
+            break;
+          }
+        }
+        const T *sl = a.slots + (K2 * a.nch) * kTB + R * RPC + h;
+        if (lane < nc) p0 = __ldcg(sl + long(lane) * kTB);
+        if (lane + 32 < nc) p1 = __ldcg(sl + long(lane + 32) * kTB);
+        for (int cc = lane + 64; cc < nc; cc += 32) pmore += __ldcg(sl + long(cc) * kTB);
+      }
+    }
+    // the last two blocks
+    for (long m = nb - 2 < 0 ? 0 : nb - 2; m < nb; ++m) {
+      bar_wait(sh_u32(&S.e2bar[m & 3]), uint32_t((m >> 2) & 1), a.status, dead);
+      if (h == RPC - 1 && m % CS == R) publish(m);
+    }
+    cp_wait<0>();
+  }
+  cl.sync();  // no CTA leaves while a peer may still write into its shared memory
+}
+
 template <typename T, int CS>
 __global__ void __launch_bounds__(kNT, 1) trsv_cluster_kernel(Args<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -414,9 +702,12 @@ __global__ void __launch_bounds__(kNT, 1) trsv_cluster_kernel(Args<T> a) {
   const int role = *cl.map_shared_rank(&s_role, 0);
   cl.sync();
   bool dead = false;
-  if (role == 1)
-    solve_chain<T, CS>(a, *reinterpret_cast<SmemSolver<T, CS> *>(smem_raw), dead);
-  else
+  if (role == 1) {
+    if constexpr (CS == kCS2)
+      solve_chain2<T>(a, *reinterpret_cast<SmemSolver2<T> *>(smem_raw), dead);
+    else
+      solve_chain<T, CS>(a, *reinterpret_cast<SmemSolver<T, CS> *>(smem_raw), dead);
+  } else
     stream_items<T>(a, *reinterpret_cast<SmemStream<T> *>(smem_raw), dead);
 }
 
@@ -476,7 +767,8 @@ __global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
 
 template <typename T, int CS>
 size_t trsv_cluster_smem() {
-  const size_t a = sizeof(tc::SmemSolver<T, CS>), b = sizeof(tc::SmemStream<T>);
+  const size_t a = CS == tc::kCS2 ? sizeof(tc::SmemSolver2<T>) : sizeof(tc::SmemSolver<T, CS>);
+  const size_t b = sizeof(tc::SmemStream<T>);
   size_t s = a > b ? a : b;
   // more than half an SM's shared memory, so a solver CTA never shares its
   // SM (and FP64 pipe) with a streaming CTA
@@ -572,6 +864,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   a.rev = upper != trans;
   a.trans = trans;
   a.unit = unit;
+  a.vec16 = !a.rev && !trans && (lda * long(sizeof(T))) % 16 == 0 && aligned16(A);
   EXB_CUDA(cudaMemsetAsync(a.xflag, 0, flag_b, c.stream));
   trsv_inverse_kernel<T><<<nb, kNT, 0, c.stream>>>(a);
   EXB_LAUNCH("trsv inverse kernel");
