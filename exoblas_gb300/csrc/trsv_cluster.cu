@@ -436,7 +436,7 @@ struct SmemSolver2 {
   T bvals[kPre][kRPC2];
   T rfull[2][kTB];
   T xring[kXR][kTB];
-  T carry[2][kRPC2];
+  T carry[2][kRPC2][32];  // per-lane partial sums of the carry, added inside the critical row dot
   unsigned long long e1bar[2];
   unsigned long long e2bar[4];
   unsigned long long cready[2];
@@ -516,7 +516,7 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) bar_init(sh_u32(&S.e1bar[i]), 1);
     for (int i = 0; i < 4; ++i) bar_init(sh_u32(&S.e2bar[i]), 1);
-    for (int i = 0; i < 2; ++i) bar_init(sh_u32(&S.cready[i]), 4);
+    for (int i = 0; i < 2; ++i) bar_init(sh_u32(&S.cready[i]), 32 * (kNT / 32 - RPC));  // every helper lane
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     for (int i = 0; i < 2; ++i) arm(sh_u32(&S.e1bar[i]), kXBytes);
     for (int i = 0; i < 4; ++i) arm(sh_u32(&S.e2bar[i]), kXBytes);
@@ -537,13 +537,18 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
     for (long K = 0; K < nb; ++K) {
       bar_wait(sh_u32(&S.cready[K & 1]), uint32_t((K >> 1) & 1), a.status, dead);
       const T *st = S.stage[K % kPre];
-      T t0 = T(0);
+      // carry + L[K,K-1] x_{K-1}: the helpers' per-lane partials start the
+      // lane sums, so one tree reduces both
+      T s = S.carry[K & 1][w][lane];
       if (K >= 1) {
         bar_wait(sh_u32(&S.e2bar[(K - 1) & 3]), uint32_t(((K - 1) >> 2) & 1), a.status, dead);
         if (w == 0 && lane == 0) arm(sh_u32(&S.e2bar[(K - 1) & 3]), kXBytes);  // for step K+3
-        t0 = rowdot(st + w * kTB, S.xring[(K - 1) % kXR]);
+        const T *row = st + w * kTB, *xv = S.xring[(K - 1) % kXR];
+        s = fma(row[lane + 32], xv[lane + 32], fma(row[lane], xv[lane], s));
       }
-      const T rr = S.bvals[K % kPre][w] - S.carry[K & 1][w] - t0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      const T rr = S.bvals[K % kPre][w] - s;
       if (lane < CS)  // lane d hands the residual to CTA d
         st_async(map_rank(sh_u32(&S.rfull[K & 1][R * RPC + w]), lane), rr, map_rank(sh_u32(&S.e1bar[K & 1]), lane));
       bar_wait(sh_u32(&S.e1bar[K & 1]), uint32_t((K >> 1) & 1), a.status, dead);
@@ -617,10 +622,8 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
     for (int p = 0; p < kPre; ++p) prefetch(p);
     cp_wait<kPre - 1>();
     helper_sync();
-    if (lane == 0) {
-      S.carry[0][h] = T(0);
-      arrive_local(sh_u32(&S.cready[0]));
-    }
+    S.carry[0][h][lane] = T(0);
+    arrive_local(sh_u32(&S.cready[0]));
     // bulk slots of the row being prepared, loaded one iteration ahead so
     // the loads are in flight while other work runs (lane c: slots c, c + 32)
     T p0 = T(0), p1 = T(0), pmore = T(0);
@@ -651,13 +654,8 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
         s0 = fma(row[lane], xv[lane], s0);
         s1 = fma(row[lane + 32], xv[lane + 32], s1);
       }
-      T sum = (s0 + s1) + ((p0 + p1) + pmore);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0) {
-        S.carry[T1 & 1][h] = sum;
-        arrive_local(sh_u32(&S.cready[T1 & 1]));
-      }
+      S.carry[T1 & 1][h][lane] = (s0 + s1) + ((p0 + p1) + pmore);
+      arrive_local(sh_u32(&S.cready[T1 & 1]));
       // bulk slots of row T1 + 1, added in the next iteration
       p0 = p1 = pmore = T(0);
       const long K2 = T1 + 1;
