@@ -68,6 +68,9 @@ L3 = {
     "exo_dsymm": ("v", "iiiiidpipidpi"),
     "exo_ssyrk": ("v", "iiiiifpifpi"),
     "exo_dsyrk": ("v", "iiiiidpidpi"),
+    "exo_ssyr2k": ("v", "iiiiifpipifpi"),
+    "exo_dsyr2k": ("v", "iiiiidpipidpi"),
+    "exo_strmm": ("v", "iiiiiiifpipi"),
 }
 EXTRA = {
     "exoblas_get_status": ("i", ""),

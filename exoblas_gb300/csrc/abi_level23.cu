@@ -76,6 +76,20 @@ static void syrk_dispatch(bool upper, bool trans, long n, long k, double alpha, 
     return;
   l3::syrk_simt<double>(upper, trans, n, k, alpha, A, lda, beta, C, ldc);
 }
+static void syr2k_dispatch(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda,
+                           const float *B, long ldb, float beta, float *C, long ldc) {
+  if (split_mode() && k > 0)
+    l3::syr2k_split_bf16(upper, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+  else
+    l3::syr2k_simt<float>(upper, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+static void syr2k_dispatch(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda,
+                           const double *B, long ldb, double beta, double *C, long ldc) {
+  if (ctx().precision == EXOBLAS_PRECISION_OZAKI && k > 0 &&
+      l3::dsyr2k_ozaki(upper, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc))
+    return;
+  l3::syr2k_simt<double>(upper, trans, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+}
 
 // ------------------------------------------------------------------ level 2
 
@@ -286,6 +300,54 @@ static void syrk_entry(const char *fn, int Order, int Uplo, int Trans, int N, in
   });
 }
 
+// test/level3/syr2k/exo_syr2k_wrapper.h:9-32.  Uplo other than Upper or Lower
+// leaves C unchanged, as neither branch of the proc's guard
+// (src/level3/syr2k.py:33) and of trmscal (src/level3/mscal.py:26) holds.
+template <typename T>
+static void syr2k_entry(const char *fn, int Order, int Uplo, int Trans, int N, int K, T alpha, const T *A, int lda,
+                        const T *B, int ldb, T beta, T *C, int ldc) {
+  guarded(fn, [&] {
+    row_major(Order);
+    nonneg(N, "N < 0");
+    nonneg(K, "K < 0");
+    if (N == 0 || (Uplo != kUpper && Uplo != kLower)) return;
+    const bool trans = Trans != kNoTrans;
+    const long ar = trans ? K : N, ac = trans ? N : K;
+    if (K > 0) {
+      ld_ok(lda, ac, "lda too small");
+      ld_ok(ldb, ac, "ldb too small");
+    }
+    ld_ok(ldc, N, "ldc < max(1, N)");
+    Stager st;
+    const T *dA = K > 0 ? st.mat(A, ar, ac, lda, false) : A;
+    const T *dB = K > 0 ? st.mat(B, ar, ac, ldb, false) : B;
+    T *dC = st.mat(C, N, N, ldc, true);
+    syr2k_dispatch(Uplo == kUpper, trans, N, K, alpha, dA, lda, dB, ldb, beta, dC, ldc);
+    st.finish();
+  });
+}
+
+// test/level3/strmm/exo_strmm.h:7-58: Left only (the reference's Right
+// branches are empty); Diag is unit only when it equals CblasUnit.
+template <typename T>
+static void trmm_entry(const char *fn, int Order, int Side, int Uplo, int TransA, int Diag, int M, int N, T alpha,
+                       const T *A, int lda, T *B, int ldb) {
+  guarded(fn, [&] {
+    row_major(Order);
+    if (Side != kLeft) return;
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    if (M == 0 || N == 0) return;
+    ld_ok(lda, M, "lda < max(1, M)");
+    ld_ok(ldb, N, "ldb < max(1, N)");
+    Stager st;
+    const T *dA = st.mat(A, M, M, lda, false);
+    T *dB = st.mat(B, M, N, ldb, true);
+    l3::trmm_simt<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, M, N, alpha, dA, lda, dB, ldb);
+    st.finish();
+  });
+}
+
 }  // namespace exb
 
 using namespace exb;
@@ -386,6 +448,21 @@ void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const e
                const int N, const int K, const double alpha, const double *A, const int lda, const double beta,
                double *C, const int ldc) {
   syrk_entry<double>("exo_dsyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+void exo_ssyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+                const int N, const int K, const float alpha, const float *A, const int lda, const float *B,
+                const int ldb, const float beta, float *C, const int ldc) {
+  syr2k_entry<float>("exo_ssyr2k", Order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_dsyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+                const int N, const int K, const double alpha, const double *A, const int lda, const double *B,
+                const int ldb, const double beta, double *C, const int ldc) {
+  syr2k_entry<double>("exo_dsyr2k", Order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
+}
+void exo_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+               const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_DIAG Diag, const int M, const int N,
+               const float alpha, const float *A, const int lda, float *B, const int ldb) {
+  trmm_entry<float>("exo_strmm", Order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb);
 }
 
 }  // extern "C"

@@ -6,7 +6,7 @@
 // the store, replacing the reference's separate mscal / trmscal pass
 // (test/level3/*/exo_*_wrapper.h, src/level3/mscal.py:12-28); it is applied
 // as a multiplication even when beta == 0, as that pass does.
-// Reference algorithms: src/level3/{gemm,symm,syrk}.py.
+// Reference algorithms: src/level3/{gemm,symm,syrk,syr2k,trmm}.py.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -38,6 +38,33 @@ struct Sym {  // symmetric matrix from its stored triangle
 };
 
 template <typename T>
+struct Cat {  // [op(X) | op(Y)]: columns c < K from X, the rest from Y (syr2k)
+  Plain<T> x, y;
+  long K;
+  __device__ __forceinline__ T operator()(long r, long c) const { return c < K ? x(r, c) : y(r, c - K); }
+  __device__ __forceinline__ bool contiguous_cols() const { return x.contiguous_cols(); }
+};
+template <typename T, class V>
+struct Transposed {  // element (r, c) of V^T
+  V v;
+  __device__ __forceinline__ T operator()(long r, long c) const { return v(c, r); }
+  __device__ __forceinline__ bool contiguous_cols() const { return !v.contiguous_cols(); }
+};
+template <typename T>
+struct Tri {  // op(A) for a triangular A: zero outside the stored triangle, ones on a unit diagonal
+  const T *p;
+  long ld;
+  bool upper, trans, unit;
+  __device__ __forceinline__ T operator()(long r, long c) const {
+    const long i = trans ? c : r, j = trans ? r : c;  // A's own row / column
+    if (i == j) return unit ? T(1) : p[i * ld + i];
+    const bool stored = upper ? j > i : j < i;
+    return stored ? p[i * ld + j] : T(0);
+  }
+  __device__ __forceinline__ bool contiguous_cols() const { return !trans; }
+};
+
+template <typename T>
 struct Cfg;
 template <>
 struct Cfg<float> {
@@ -48,12 +75,14 @@ struct Cfg<double> {
   static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4, THREADS = 256;
 };
 
-// C tile (bm, bn) of rows m x cols n.  tri: 0 all tiles, 1 lower, 2 upper
-// (syrk): tiles strictly outside the triangle are not launched and elements
-// outside it are left untouched.
+// C tile (bm, bn) of rows m x cols n.  mode & 3: 0 all tiles, 1 lower,
+// 2 upper (syrk): tiles strictly outside the triangle are not launched and
+// elements outside it are left untouched.  mode & 4: C = alpha * acc without
+// reading C (trmm overwrites its operand).
 template <typename T, class OA, class OB>
 __global__ void __launch_bounds__(Cfg<T>::THREADS)
-    gemm_kernel(long m, long n, long k, T alpha, OA opA, OB opB, T beta, T *C, long ldc, int tri) {
+    gemm_kernel(long m, long n, long k, T alpha, OA opA, OB opB, T beta, T *C, long ldc, int mode) {
+  const int tri = mode & 3;
   constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN, BK = Cfg<T>::BK, TM = Cfg<T>::TM, TN = Cfg<T>::TN;
   constexpr int NT = Cfg<T>::THREADS;
   constexpr int LA = BM * BK / NT, LB = BN * BK / NT;  // loads per thread per tile
@@ -163,23 +192,23 @@ __global__ void __launch_bounds__(Cfg<T>::THREADS)
       if (tri == 1 && gj > gi) continue;
       if (tri == 2 && gj < gi) continue;
       T *c = C + gi * ldc + gj;
-      *c = alpha * acc[a][b] + beta * *c;
+      *c = (mode & 4) ? alpha * acc[a][b] : alpha * acc[a][b] + beta * *c;
     }
   }
 }
 
 template <typename T, class OA, class OB>
-static void launch(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int tri) {
+static void launch(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int mode) {
   constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN;
   if (m <= 0 || n <= 0) return;
   dim3 grid;
-  if (tri == 0) {
+  if ((mode & 3) == 0) {
     grid = dim3(unsigned(ceil_div(n, BN)), unsigned(ceil_div(m, BM)));
   } else {
     const long nt = ceil_div(n, BM);  // BM == BN for every configuration
     grid = dim3(unsigned(nt * (nt + 1) / 2));
   }
-  gemm_kernel<T, OA, OB><<<grid, Cfg<T>::THREADS, 0, ctx().stream>>>(m, n, k, alpha, a, b, beta, C, ldc, tri);
+  gemm_kernel<T, OA, OB><<<grid, Cfg<T>::THREADS, 0, ctx().stream>>>(m, n, k, alpha, a, b, beta, C, ldc, mode);
   EXB_LAUNCH("gemm kernel");
   count_launch();
 }
@@ -208,6 +237,36 @@ void syrk_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long
   launch<T>(n, n, k, alpha, Plain<T>{A, lda, trans}, Plain<T>{A, lda, !trans}, beta, C, ldc, upper ? 2 : 1);
 }
 
+// src/level3/syr2k.py:14-37: C_tri = alpha (op(A) op(B)^T + op(B) op(A)^T)
+// + beta C_tri, one product of [op(A) | op(B)] (n x 2k) with [op(B) | op(A)]^T
+template <typename T>
+void syr2k_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+                T *C, long ldc) {
+  const Cat<T> ab{Plain<T>{A, lda, trans}, Plain<T>{B, ldb, trans}, k};
+  const Cat<T> ba{Plain<T>{B, ldb, trans}, Plain<T>{A, lda, trans}, k};
+  launch<T>(n, n, 2 * k, alpha, ab, Transposed<T, Cat<T>>{ba}, beta, C, ldc, upper ? 2 : 1);
+}
+
+// src/level3/trmm.py:12-78 (Left): B = alpha op(A) B with A triangular.  B
+// is copied to scratch first (the product reads every row of B while it is
+// overwritten).  Entries outside the triangle enter the product as zeros, so
+// an infinity or NaN in B reaches rows whose triangle excludes it; the
+// reference skips those terms.
+template <typename T>
+void trmm_simt(bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B, long ldb) {
+  if (m <= 0 || n <= 0) return;
+  T *Bc = static_cast<T *>(scratch(sizeof(T) * size_t(m) * size_t(n)));
+  EXB_CUDA(cudaMemcpy2DAsync(Bc, sizeof(T) * size_t(n), B, sizeof(T) * size_t(ldb), sizeof(T) * size_t(n), size_t(m),
+                             cudaMemcpyDeviceToDevice, ctx().stream));
+  launch<T>(m, n, m, alpha, Tri<T>{A, lda, upper, trans, unit}, Plain<T>{Bc, n, false}, T(0), B, ldb, 4);
+}
+
+template void syr2k_simt<float>(bool, bool, long, long, float, const float *, long, const float *, long, float,
+                                float *, long);
+template void syr2k_simt<double>(bool, bool, long, long, double, const double *, long, const double *, long, double,
+                                 double *, long);
+template void trmm_simt<float>(bool, bool, bool, long, long, float, const float *, long, float *, long);
+template void trmm_simt<double>(bool, bool, bool, long, long, double, const double *, long, double *, long);
 template void gemm_simt<float>(bool, bool, long, long, long, float, const float *, long, const float *, long, float,
                                float *, long);
 template void gemm_simt<double>(bool, bool, long, long, long, double, const double *, long, const double *, long,

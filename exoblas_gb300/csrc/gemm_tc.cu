@@ -323,6 +323,12 @@ struct ViewPlain {
   __device__ float operator()(int r, int k) const { return t ? p[long(k) * ld + r] : p[long(r) * ld + k]; }
   __device__ bool k_contiguous() const { return !t; }
 };
+struct ViewCat {  // [X | Y]: k < K from X, the rest from Y (syr2k)
+  ViewPlain x, y;
+  int K;
+  __device__ float operator()(int r, int k) const { return k < K ? x(r, k) : y(r, k - K); }
+  __device__ bool k_contiguous() const { return x.k_contiguous(); }
+};
 struct ViewSym {
   const float *p;
   long ld;
@@ -416,6 +422,15 @@ void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const 
   // X_A = op(A) (n x k): NoTrans row i of A, Trans column i of A
   t5::ViewPlain x{A, lda, trans};
   t5::run(x, x, int(n), int(n), int(k), alpha, beta, C, ldc, upper ? 2 : 1, true);
+}
+
+void syr2k_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, const float *B,
+                      long ldb, float beta, float *C, long ldc) {
+  if (n <= 0) return;
+  // X_A = [op(A) | op(B)], X_B = [op(B) | op(A)] (n x 2k each)
+  const t5::ViewPlain a{A, lda, trans}, b{B, ldb, trans};
+  t5::run(t5::ViewCat{a, b, int(k)}, t5::ViewCat{b, a, int(k)}, int(n), int(n), int(2 * k), alpha, beta, C, ldc,
+          upper ? 2 : 1, false);
 }
 
 }  // namespace l3

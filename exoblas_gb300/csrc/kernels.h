@@ -60,6 +60,11 @@ void symm_simt(bool left, bool upper, long m, long n, T alpha, const T *A, long 
                T *C, long ldc);
 template <typename T>
 void syrk_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, T beta, T *C, long ldc);
+template <typename T>
+void syr2k_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
+                T *C, long ldc);
+template <typename T>
+void trmm_simt(bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B, long ldb);
 // tcgen05 tensor-core paths: FP32 through three BF16 terms per operand
 void gemm_split_bf16(bool ta, bool tb, long m, long n, long k, float alpha, const float *A, long lda, const float *B,
                      long ldb, float beta, float *C, long ldc);
@@ -67,6 +72,8 @@ void symm_split_bf16(bool left, bool upper, long m, long n, float alpha, const f
                      long ldb, float beta, float *C, long ldc);
 void syrk_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, float beta,
                      float *C, long ldc);
+void syr2k_split_bf16(bool upper, bool trans, long n, long k, float alpha, const float *A, long lda, const float *B,
+                      long ldb, float beta, float *C, long ldc);
 // tcgen05 Ozaki slice emulation of dgemm; false when an input is not finite
 // (nothing written; the caller uses the FP64 FMA kernel)
 bool dgemm_ozaki(bool ta, bool tb, long m, long n, long k, double alpha, const double *A, long lda, const double *B,
@@ -75,6 +82,8 @@ bool dsymm_ozaki(bool left, bool upper, long m, long n, double alpha, const doub
                  long ldb, double beta, double *C, long ldc);
 bool dsyrk_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, double beta,
                  double *C, long ldc);
+bool dsyr2k_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, const double *B,
+                  long ldb, double beta, double *C, long ldc);
 }  // namespace l3
 
 }  // namespace exb

@@ -259,7 +259,12 @@ struct View {  // X(r, k) of the logical rows x K operand
   long ld;
   bool t;       // element (r, k) at p[k * ld + r]
   int sym = 0;  // 1 / 2: symmetric, only the upper / lower triangle stored
+  // columns k >= ks come from a second operand q (same orientation; syr2k)
+  const double *q = nullptr;
+  long ldq = 0;
+  int ks = 1 << 30;
   __device__ double operator()(int r, int k) const {
+    if (k >= ks) return t ? q[long(k - ks) * ldq + r] : q[long(r) * ldq + (k - ks)];
     if (sym) {
       const bool direct = sym == 1 ? r <= k : r >= k;
       return direct ? p[long(r) * ld + k] : p[long(k) * ld + r];
@@ -382,13 +387,12 @@ static void init_products() {
 // Returns false (nothing written) when an input holds NaN or infinity; the
 // caller then uses the FP64 FMA kernel, which propagates them.
 // C[M, N] = alpha X_A X_B^T + beta C with X_A (M x K) and X_B (N x K).
-// tri != 0 (syrk): X_B is X_A, N == M, only that triangle of C is written;
-// the operand is scaled and sliced once.
+// tri != 0 (syrk, syr2k): N == M and only that triangle of C is written;
+// same_ab (syrk): X_B is X_A, scaled and sliced once.
 static bool run(const View &xa, const View &xb, int M, int N, int K, double alpha, double beta, double *C, long ldc,
-                int tri) {
+                int tri, bool same_ab) {
   Context &c = ctx();
   init_products();
-  const bool same_ab = tri != 0;
   const int Kp = round_up(K, BK * kChunkKB), Mp = round_up(M, BM), Np = tri ? Mp : round_up(N, BN);
   const size_t a_elems = size_t(kS) * Mp * Kp, b_elems = same_ab ? 0 : size_t(kS) * Np * Kp;
   const size_t ebytes = (size_t(Mp + Np + 64) * 4 + 255) & ~size_t(255);
@@ -454,7 +458,7 @@ bool dgemm_ozaki(bool ta, bool tb, long m, long n, long k, double alpha, const d
                  long ldb, double beta, double *C, long ldc) {
   if (m <= 0 || n <= 0 || k <= 0) return false;
   // X_A = op(A); X_B(j, k) = op(B)[k][j]
-  return oz::run(oz::View{A, lda, ta}, oz::View{B, ldb, !tb}, int(m), int(n), int(k), alpha, beta, C, ldc, 0);
+  return oz::run(oz::View{A, lda, ta}, oz::View{B, ldb, !tb}, int(m), int(n), int(k), alpha, beta, C, ldc, 0, false);
 }
 
 // C_tri = alpha op(A) op(A)^T + beta C_tri over the stored triangle only
@@ -463,7 +467,16 @@ bool dsyrk_ozaki(bool upper, bool trans, long n, long k, double alpha, const dou
                  double *C, long ldc) {
   if (n <= 0 || k <= 0) return false;
   const oz::View x{A, lda, trans};
-  return oz::run(x, x, int(n), int(n), int(k), alpha, beta, C, ldc, upper ? 2 : 1);
+  return oz::run(x, x, int(n), int(n), int(k), alpha, beta, C, ldc, upper ? 2 : 1, true);
+}
+
+// C_tri = alpha (op(A) op(B)^T + op(B) op(A)^T) + beta C_tri (syr2k) as the
+// triangle of [op(A) | op(B)] [op(B) | op(A)]^T
+bool dsyr2k_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, const double *B,
+                  long ldb, double beta, double *C, long ldc) {
+  if (n <= 0 || k <= 0) return false;
+  const oz::View ab{A, lda, trans, 0, B, ldb, int(k)}, ba{B, ldb, trans, 0, A, lda, int(k)};
+  return oz::run(ab, ba, int(n), int(n), int(2 * k), alpha, beta, C, ldc, upper ? 2 : 1, false);
 }
 
 // C = alpha sym(A) B + beta C (left) or alpha B sym(A) + beta C (right),
@@ -472,8 +485,8 @@ bool dsymm_ozaki(bool left, bool upper, long m, long n, double alpha, const doub
                  long ldb, double beta, double *C, long ldc) {
   if (m <= 0 || n <= 0) return false;
   const oz::View sa{A, lda, false, upper ? 1 : 2};
-  if (left) return oz::run(sa, oz::View{B, ldb, true}, int(m), int(n), int(m), alpha, beta, C, ldc, 0);
-  return oz::run(oz::View{B, ldb, false}, sa, int(m), int(n), int(n), alpha, beta, C, ldc, 0);
+  if (left) return oz::run(sa, oz::View{B, ldb, true}, int(m), int(n), int(m), alpha, beta, C, ldc, 0, false);
+  return oz::run(oz::View{B, ldb, false}, sa, int(m), int(n), int(n), alpha, beta, C, ldc, 0, false);
 }
 
 }  // namespace l3

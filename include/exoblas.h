@@ -85,12 +85,12 @@ EXOBLAS_API int exoblas_set_blocking(int blocking);
  * kernel queued in non-blocking mode (trsv) gave up a bounded wait. */
 EXOBLAS_API int exoblas_synchronize(void);
 
-/* Arithmetic used by exo_sgemm/ssymm/ssyrk and exo_dgemm/dsymm/dsyrk:
+/* Arithmetic used by exo_sgemm/ssymm/ssyrk/ssyr2k and exo_dgemm/dsymm/dsyrk/dsyr2k:
  *   EXOBLAS_PRECISION_NATIVE    FP32 FFMA / FP64 DFMA kernels (default)
- *   EXOBLAS_PRECISION_SPLIT_BF16 sgemm/ssymm/ssyrk: each FP32 operand split
+ *   EXOBLAS_PRECISION_SPLIT_BF16 sgemm/ssymm/ssyrk/ssyr2k: each FP32 operand split
  *                               into three BF16 terms, products on tcgen05
  *                               tensor cores, FP32 accumulation
- *   EXOBLAS_PRECISION_OZAKI     dgemm/dsymm/dsyrk: Ozaki slice emulation
+ *   EXOBLAS_PRECISION_OZAKI     dgemm/dsymm/dsyrk/dsyr2k: Ozaki slice emulation
  *                               with exact integer accumulation of
  *                               small-integer slices (inputs holding NaN or
  *                               infinity take the DFMA kernels)
@@ -224,6 +224,19 @@ EXOBLAS_API void exo_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO U
 EXOBLAS_API void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans, const int N,
                const int K, const double alpha, const double *A, const int lda, const double beta, double *C,
                const int ldc);
+/* test/level3/syr2k/exo_syr2k_wrapper.h:9-32 (the triangle of C *= beta, then
+ * C_tri += alpha (op(A) op(B)^T + op(B) op(A)^T)) */
+EXOBLAS_API void exo_ssyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+               const int N, const int K, const float alpha, const float *A, const int lda, const float *B,
+               const int ldb, const float beta, float *C, const int ldc);
+EXOBLAS_API void exo_dsyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
+               const int N, const int K, const double alpha, const double *A, const int lda, const double *B,
+               const int ldb, const double beta, double *C, const int ldc);
+/* test/level3/strmm/exo_strmm.h:7-58 (B = alpha op(A) B, A triangular, Side
+ * Left; like the reference, Side Right leaves B unchanged) */
+EXOBLAS_API void exo_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
+               const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_DIAG Diag, const int M, const int N,
+               const float alpha, const float *A, const int lda, float *B, const int ldb);
 
 /* ------------------------------------------------------------ batching --- */
 /* Many independent exo_sgemm / exo_dgemv / exo_strsv calls of uneven sizes

@@ -91,6 +91,10 @@ SIGS = {
     "oracle_dsymm": ("v", "iiiiidpipidpi"),
     "oracle_ssyrk": ("v", "iiiiifpifpi"),
     "oracle_dsyrk": ("v", "iiiiidpidpi"),
+    "oracle_ssyr2k": ("v", "iiiiifpipifpi"),
+    "oracle_dsyr2k": ("v", "iiiiidpipidpi"),
+    "oracle_strmm": ("v", "iiiiiiifpipi"),
+    "oracle_dtrmm": ("v", "iiiiiiidpipi"),
     "oracle_dd_dot": ("d", "lplpl"),
     "oracle_dd_gemv": ("v", "illdplpdpp"),
     "oracle_dd_trsv": ("v", "iiilplpp"),

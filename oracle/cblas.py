@@ -35,6 +35,8 @@ SIGS = {
     "sgemm": ("v", "iiiiiifpipifpi"), "dgemm": ("v", "iiiiiidpipidpi"),
     "ssymm": ("v", "iiiiifpipifpi"), "dsymm": ("v", "iiiiidpipidpi"),
     "ssyrk": ("v", "iiiiifpifpi"), "dsyrk": ("v", "iiiiidpidpi"),
+    "ssyr2k": ("v", "iiiiifpipifpi"), "dsyr2k": ("v", "iiiiidpipidpi"),
+    "strmm": ("v", "iiiiiiifpipi"), "dtrmm": ("v", "iiiiiiidpipi"),
 }
 
 _lib = None

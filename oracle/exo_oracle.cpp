@@ -10,7 +10,7 @@
 // Each function cites the reference file:line it follows.  Sources:
 //   src/level1/{asum,axpy,dot,dsdot,exo_copy,rot,rotm,scal,swap}.py
 //   src/level2/{gemv,ger,symv,syr,syr2,trmv,trsv}.py
-//   src/level3/{gemm,symm,syrk,mscal}.py
+//   src/level3/{gemm,symm,syrk,syr2k,trmm,mscal}.py
 //   test/level*/<op>/exo_<op>_wrapper.h, test/level1/sdsdot/exo_sdsdot.h
 //
 // The reference raises a C++ exception when Order != RowMajor.  The oracle
@@ -575,6 +575,82 @@ void syrk_wrap(int order, int Uplo, int Trans, int N, int K, T alpha,
   syrk_rows<T>(Uplo, Trans, 0, N, N, K, alpha, a, c);
 }
 
+// src/level3/syr2k.py:14-37: C[i,j] += alpha * (A[i,k] B[j,k] + B[i,k] A[j,k])
+// over the stored triangle (NoTrans), with A^T / B^T read as AT[k,i] (Trans)
+template <typename T>
+void syr2k_rows(int Uplo, int Trans, long i0, long i1, long N, long K, T alpha, Mat<T> a, Mat<T> b, Mat<T> c) {
+  if (Uplo != kUpper && Uplo != kLower) return;  // neither branch of the proc's guard
+  for (long i = i0; i < i1; ++i) {
+    const long j0 = Uplo == kUpper ? i : 0;
+    const long j1 = Uplo == kUpper ? N : i + 1;
+    for (long j = j0; j < j1; ++j) {
+      T acc = c(i, j);
+      for (long k = 0; k < K; ++k) {
+        if (Trans == kNoTrans)
+          acc += alpha * (a(i, k) * b(j, k) + b(i, k) * a(j, k));
+        else
+          acc += alpha * (a(k, i) * b(k, j) + b(k, i) * a(k, j));
+      }
+      c(i, j) = acc;
+    }
+  }
+}
+
+// test/level3/syr2k/exo_syr2k_wrapper.h:9-32: trmscal then the proc
+template <typename T>
+void syr2k_wrap(int order, int Uplo, int Trans, int N, int K, T alpha, const T *A, int lda, const T *B, int ldb,
+                T beta, T *C, int ldc) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  Mat<T> a{const_cast<T *>(A), lda}, b{const_cast<T *>(B), ldb}, c{C, ldc};
+  trmscal_proc<T>(Uplo, N, beta, c);
+  syr2k_rows<T>(Uplo, Trans, 0, N, N, K, alpha, a, b, c);
+}
+
+// src/level3/trmm.py:12-78, the four Left procs exactly in their loop order
+// (unit diagonal when `unit`); B = alpha op(A) B in place.
+template <typename T>
+void trmm_left(bool upper, bool trans, bool unit, long m, long n, T alpha, Mat<T> a, Mat<T> b) {
+  const bool forward = upper != trans;  // Upper/NonTrans and Lower/Trans walk i upwards
+  for (long j = 0; j < n; ++j) {
+    for (long i = 0; i < m; ++i) {
+      if (forward) {
+        if (!unit) b(i, j) = a(i, i) * b(i, j);
+        for (long k = 0; k < m - i - 1; ++k) {
+          const T aik = upper ? a(i, i + k + 1) : a(i + k + 1, i);
+          b(i, j) += aik * b(i + k + 1, j);
+        }
+        b(i, j) = alpha * b(i, j);
+      } else {
+        const long r = m - i - 1;
+        const T org = b(r, j);
+        b(r, j) = T(0);
+        for (long k = 0; k < r; ++k) {
+          const T ark = upper ? a(k, r) : a(r, k);
+          b(r, j) += ark * b(k, j);
+        }
+        if (!unit)
+          b(r, j) += a(r, r) * org;
+        else
+          b(r, j) += org;
+        b(r, j) = alpha * b(r, j);
+      }
+    }
+  }
+}
+
+// test/level3/strmm/exo_strmm.h:7-58: Left dispatches on Uplo / TransA; the
+// Right side does nothing; Diag is unit only when it equals CblasUnit.
+template <typename T>
+void trmm_wrap(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, T alpha, const T *A, int lda, T *B,
+               int ldb) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  if (Side != kLeft) return;
+  Mat<T> a{const_cast<T *>(A), lda}, b{B, ldb};
+  trmm_left<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, M, N, alpha, a, b);
+}
+
 // --------------------------------------------------- double-double oracle --
 // TwoSum (Knuth, TAOCP vol. 2), TwoProd through fma (Dekker 1971),
 // Dot2 (Ogita, Rump, Oishi, "Accurate sum and dot product", SISC 2005).
@@ -720,6 +796,11 @@ ORACLE_API void oracle_ssymm(int order, int Side, int Uplo, int M, int N, float 
 ORACLE_API void oracle_dsymm(int order, int Side, int Uplo, int M, int N, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { symm_wrap<double>(order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc); }
 ORACLE_API void oracle_ssyrk(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, float beta, float *C, int ldc) { syrk_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
 ORACLE_API void oracle_dsyrk(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, double beta, double *C, int ldc) { syrk_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
+
+ORACLE_API void oracle_ssyr2k(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc) { syr2k_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dsyr2k(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { syr2k_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_strmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, float alpha, const float *A, int lda, float *B, int ldb) { trmm_wrap<float>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }
+ORACLE_API void oracle_dtrmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, double alpha, const double *A, int lda, double *B, int ldb) { trmm_wrap<double>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }
 
 // ----- double-double high-precision references (results rounded to double)
 

@@ -241,3 +241,26 @@ def syrk_cases(p, dims=L3_DIMS, ldds=(0, 5)):
         A, C = mat(g, ar, lda, DT[p]), mat(g, n, ldc, DT[p])
         yield Case(p + "syrk", [ROW, u, t, n, k, 13.0, A, lda, 18.0, C, ldc], [9], nred=k + 1,
                    label=f"n={n} k={k} t={t} u={u} ldd={ldd}")
+
+
+def syr2k_cases(p, dims=L3_DIMS, ldds=(0, 5)):
+    """test/level3/syr2k/correctness.cpp:13-62 (alpha 13, beta 18)"""
+    for u, n, k, t, da, db, dc in itertools.product((LO, UP), dims, dims, (NT, TR), ldds, ldds, ldds):
+        g = rng(_seed("syr2k", p, u, n, k, t, da, db, dc))
+        ar, ac = (n, k) if t == NT else (k, n)
+        lda, ldb, ldc = ac + da, ac + db, n + dc
+        A, B, C = mat(g, ar, lda, DT[p]), mat(g, ar, ldb, DT[p]), mat(g, n, ldc, DT[p])
+        yield Case(p + "syr2k", [ROW, u, t, n, k, 13.0, A, lda, B, ldb, 18.0, C, ldc], [11], nred=2 * k + 1,
+                   label=f"u={u} n={n} k={k} t={t} lda={lda} ldb={ldb} ldc={ldc}")
+
+
+def trmm_cases(Ms=(4, 101, 321), Ns=(8, 15, 564), alphas=(0.0, 1.0, 1.4), ldds=(0, 5)):
+    """test/level3/strmm/correctness.cpp:11-80 (float only, Side Left; A and
+    B are AlignedBuffer(K * lda) / AlignedBuffer(M * ldb) of uniform[-1, 1))"""
+    for m, n, u, t, d, al, da, db in itertools.product(Ms, Ns, (UP, LO), (NT, TR), (NU, UN), alphas, ldds, ldds):
+        g = rng(_seed("trmm", m, n, u, t, d, al, da, db))
+        lda, ldb = m + da, n + db
+        A, B = mat(g, m, lda, np.float32), mat(g, m, ldb, np.float32)
+        yield Case("strmm", [ROW, LEFT, u, t, d, m, n, al, A, lda, B, ldb], [10], nred=m + 1,
+                   label=f"m={m} n={n} u={u} t={t} d={d} alpha={al} lda={lda} ldb={ldb}")
+

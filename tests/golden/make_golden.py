@@ -52,6 +52,8 @@ def families():
     f["gemm"] = subset((c for p in "sd" for c in C.gemm_cases(p, dims=(1, 7, 32, 64))), 7)
     f["symm"] = subset((c for p in "sd" for c in C.symm_cases(p, dims=(1, 7, 32, 64))), 5)
     f["syrk"] = subset((c for p in "sd" for c in C.syrk_cases(p, dims=(1, 7, 32, 64))), 5)
+    f["syr2k"] = subset((c for p in "sd" for c in C.syr2k_cases(p, dims=(1, 7, 32))), 7)
+    f["trmm"] = subset(C.trmm_cases(Ms=(4, 33), Ns=(8, 15)), 3)
     return f
 
 

@@ -1,13 +1,15 @@
-"""Level-3 parity on the GPU (grids of test/level3/{gemm,symm,syrk}/correctness.cpp)."""
+"""Level-3 parity on the GPU (grids of test/level3/{gemm,symm,syrk,syr2k,strmm}/correctness.cpp)."""
 import numpy as np
 import pytest
 
-from cases import gemm_cases, symm_cases, syrk_cases
+from cases import gemm_cases, symm_cases, syr2k_cases, syrk_cases, trmm_cases
 from common import EPS, check_case, run_gpu
 
 GEMM = [c for p in "sd" for c in gemm_cases(p)]
 SYMM = [c for p in "sd" for c in symm_cases(p)]
 SYRK = [c for p in "sd" for c in syrk_cases(p)]
+SYR2K = [c for p in "sd" for c in syr2k_cases(p)][::2]
+TRMM = list(trmm_cases())
 
 
 @pytest.mark.gpu
@@ -29,6 +31,36 @@ def test_symm(cuda, case):
 def test_syrk(cuda, case):
     r, a = run_gpu(case)
     check_case(case, r, a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", SYR2K, ids=lambda c: f"{c.op}-{c.label}")
+def test_syr2k(cuda, case):
+    r, a = run_gpu(case)
+    check_case(case, r, a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", TRMM, ids=lambda c: f"{c.op}-{c.label}")
+def test_strmm(cuda, case):
+    r, a = run_gpu(case)
+    check_case(case, r, a)
+
+
+@pytest.mark.gpu
+def test_strmm_right_side_and_order(cuda):
+    """Side Right leaves B unchanged and a column-major call is rejected, as
+    in test/level3/strmm/exo_strmm.h:12-14, 45-56."""
+    import exoblas_gb300 as eb
+
+    g = np.random.default_rng(3)
+    A = g.uniform(-1, 1, 16 * 16).astype(np.float32)
+    B = g.uniform(-1, 1, 16 * 8).astype(np.float32)
+    B0 = B.copy()
+    eb.exo_strmm(101, 142, 121, 111, 131, 16, 8, 1.5, A, 16, B, 8)
+    assert B.tobytes() == B0.tobytes()
+    with pytest.raises(eb.UnsupportedParameterException):
+        eb.exo_strmm(102, 141, 121, 111, 131, 16, 8, 1.5, A, 16, B, 8)
 
 
 @pytest.mark.gpu

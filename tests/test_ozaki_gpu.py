@@ -8,7 +8,7 @@ propagate as in the reference)."""
 import numpy as np
 import pytest
 
-from cases import gemm_cases, symm_cases, syrk_cases
+from cases import gemm_cases, symm_cases, syr2k_cases, syrk_cases
 from common import EPS, check_case, run_gpu
 
 
@@ -23,7 +23,8 @@ def ozaki_mode(cuda):
 
 CASES = ([c for c in gemm_cases("d", dims=(1, 7, 64, 257), ldds=(0, 5))][::3]
          + [c for c in symm_cases("d", dims=(1, 7, 64, 257))][::2]
-         + [c for c in syrk_cases("d", dims=(1, 7, 64, 257, 300))][::2])
+         + [c for c in syrk_cases("d", dims=(1, 7, 64, 257, 300))][::2]
+         + [c for c in syr2k_cases("d", dims=(1, 7, 64, 257), ldds=(0, 5))][::8])
 
 
 @pytest.mark.gpu

@@ -8,7 +8,7 @@ relative error against FP64 must be no worse than the plain FP32 path's
 import numpy as np
 import pytest
 
-from cases import gemm_cases, symm_cases, syrk_cases
+from cases import gemm_cases, symm_cases, syr2k_cases, syrk_cases
 from common import EPS, check_case, run_gpu
 
 
@@ -25,6 +25,7 @@ CASES = (
     [c for c in gemm_cases("s", dims=(1, 7, 64, 257), ldds=(0, 5))][::3]
     + [c for c in symm_cases("s", dims=(1, 7, 64, 257))][::2]
     + [c for c in syrk_cases("s", dims=(1, 7, 64, 257))][::2]
+    + [c for c in syr2k_cases("s", dims=(1, 7, 64, 257), ldds=(0, 5))][::8]
 )
 
 
