@@ -68,6 +68,14 @@ L3 = {
     "exo_dsymm": ("v", "iiiiidpipidpi"),
     "exo_ssyrk": ("v", "iiiiifpifpi"),
     "exo_dsyrk": ("v", "iiiiidpidpi"),
+    "exo_sgbmv": ("v", "iiiifpipifpi"),
+    "exo_dgbmv": ("v", "iiiidpipidpi"),
+    "exo_ssbmv": ("v", "iiiifpipifpi"),
+    "exo_dsbmv": ("v", "iiiidpipidpi"),
+    "exo_stbmv": ("v", "iiiiiipipi"),
+    "exo_dtbmv": ("v", "iiiiiipipi"),
+    "exo_stbsv": ("v", "iiiiiipipi"),
+    "exo_dtbsv": ("v", "iiiiiipipi"),
     "exo_ssyr2k": ("v", "iiiiifpipifpi"),
     "exo_dsyr2k": ("v", "iiiiidpipidpi"),
     "exo_strmm": ("v", "iiiiiiifpipi"),

@@ -300,6 +300,81 @@ static void syrk_entry(const char *fn, int Order, int Uplo, int Trans, int N, in
   });
 }
 
+// test/level2/sgbmv/exo_sgbmv.h:5-23 (no Order or Trans argument: row-major
+// NoTrans).  The reference passes negative increments through unrebased,
+// which reads before X; here they follow the CBLAS convention (rebased).
+template <typename T>
+static void gbmv_entry(const char *fn, int M, int N, int KL, int KU, T alpha, const T *A, int lda, const T *X,
+                       int incX, T beta, T *Y, int incY) {
+  guarded(fn, [&] {
+    nonneg(M, "M < 0");
+    nonneg(N, "N < 0");
+    nonneg(KL, "KL < 0");
+    nonneg(KU, "KU < 0");
+    if (M == 0) return;
+    const long width = long(KL) + KU + 1;
+    ld_ok(lda, width, "lda < KL + KU + 1");
+    inc_ok(incY, "incY == 0");
+    if (N > 0) inc_ok(incX, "incX == 0");
+    X = rebase(X, N, incX);
+    Y = rebase(Y, M, incY);
+    Stager st;
+    const T *dA = st.mat(A, M, width, lda, false);
+    const T *dx = st.vec(X, N, incX, false);
+    T *dy = st.vec(Y, M, incY, true);
+    l2::gbmv<T>(M, N, KL, KU, alpha, dA, lda, dx, incX, beta, dy, incY);
+    st.finish();
+  });
+}
+
+// test/level2/ssbmv/exo_ssbmv.h:7-52: y = beta y (when beta != 1) then
+// y += alpha A x; Uplo other than Upper reads the lower band.
+template <typename T>
+static void sbmv_entry(const char *fn, int order, int Uplo, int N, int K, T alpha, const T *A, int lda, const T *X,
+                       int incX, T beta, T *Y, int incY) {
+  guarded(fn, [&] {
+    row_major(order);
+    nonneg(N, "N < 0");
+    nonneg(K, "K < 0");
+    if (N == 0) return;
+    ld_ok(lda, long(K) + 1, "lda < K + 1");
+    inc_ok(incX, "incX == 0");
+    inc_ok(incY, "incY == 0");
+    X = rebase(X, N, incX);
+    Y = rebase(Y, N, incY);
+    Stager st;
+    const T *dA = st.mat(A, N, long(K) + 1, lda, false);
+    const T *dx = st.vec(X, N, incX, false);
+    T *dy = st.vec(Y, N, incY, true);
+    l2::sbmv<T>(Uplo == kUpper, N, K, alpha, dA, lda, dx, incX, beta, dy, incY);
+    st.finish();
+  });
+}
+
+// test/level2/stbmv/exo_stbmv.h and stbsv/exo_stbsv.h: Upper vs anything
+// else, NoTrans vs anything else, unit diagonal only for CblasUnit.
+template <typename T>
+static void tb_entry(const char *fn, bool solve, int order, int Uplo, int TransA, int Diag, int N, int K, const T *A,
+                     int lda, T *X, int incX) {
+  guarded(fn, [&] {
+    row_major(order);
+    nonneg(N, "N < 0");
+    nonneg(K, "K < 0");
+    if (N == 0) return;
+    ld_ok(lda, long(K) + 1, "lda < K + 1");
+    inc_ok(incX, "incX == 0");
+    X = rebase(X, N, incX);
+    Stager st;
+    const T *dA = st.mat(A, N, long(K) + 1, lda, false);
+    T *dx = st.vec(X, N, incX, true);
+    if (solve)
+      l2::tbsv<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, N, K, dA, lda, dx, incX);
+    else
+      l2::tbmv<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, N, K, dA, lda, dx, incX);
+    st.finish();
+  });
+}
+
 // test/level3/syr2k/exo_syr2k_wrapper.h:9-32.  Uplo other than Upper or Lower
 // leaves C unchanged, as neither branch of the proc's guard
 // (src/level3/syr2k.py:33) and of trmscal (src/level3/mscal.py:26) holds.
@@ -448,6 +523,44 @@ void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const e
                const int N, const int K, const double alpha, const double *A, const int lda, const double beta,
                double *C, const int ldc) {
   syrk_entry<double>("exo_dsyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
+}
+void exo_sgbmv(const int M, const int N, const int KL, const int KU, const float alpha, const float *A,
+               const int lda, const float *X, const int incX, const float beta, float *Y, const int incY) {
+  gbmv_entry<float>("exo_sgbmv", M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_dgbmv(const int M, const int N, const int KL, const int KU, const double alpha, const double *A,
+               const int lda, const double *X, const int incX, const double beta, double *Y, const int incY) {
+  gbmv_entry<double>("exo_dgbmv", M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_ssbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K, const float alpha,
+               const float *A, const int lda, const float *X, const int incX, const float beta, float *Y,
+               const int incY) {
+  sbmv_entry<float>("exo_ssbmv", order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_dsbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K, const double alpha,
+               const double *A, const int lda, const double *X, const int incX, const double beta, double *Y,
+               const int incY) {
+  sbmv_entry<double>("exo_dsbmv", order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY);
+}
+void exo_stbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
+               const int incX) {
+  tb_entry<float>("exo_stbmv", false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
+}
+void exo_dtbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
+               const int incX) {
+  tb_entry<double>("exo_dtbmv", false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
+}
+void exo_stbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
+               const int incX) {
+  tb_entry<float>("exo_stbsv", true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
+}
+void exo_dtbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
+               const int incX) {
+  tb_entry<double>("exo_dtbsv", true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
 }
 void exo_ssyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
                 const int N, const int K, const float alpha, const float *A, const int lda, const float *B,

@@ -48,6 +48,16 @@ template <typename T>
 void trmv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx);
 template <typename T>
 void trsv(bool upper, bool trans, bool unit, long n, const T *A, long lda, T *x, long incx);
+// banded (row-major CBLAS band storage)
+template <typename T>
+void gbmv(long m, long n, long kl, long ku, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y,
+          long incy);
+template <typename T>
+void sbmv(bool upper, long n, long k, T alpha, const T *A, long lda, const T *x, long incx, T beta, T *y, long incy);
+template <typename T>
+void tbmv(bool upper, bool trans, bool unit, long n, long k, const T *A, long lda, T *x, long incx);
+template <typename T>
+void tbsv(bool upper, bool trans, bool unit, long n, long k, const T *A, long lda, T *x, long incx);
 }  // namespace l2
 
 namespace l3 {

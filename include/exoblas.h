@@ -202,6 +202,36 @@ EXOBLAS_API int exoblas_sgemv_noalloc(const enum CBLAS_ORDER order, const enum C
                                       const int N, const float alpha, const float *A, const int lda, const float *X,
                                       const int incX, const float beta, float *Y, const int incY, void *stream);
 
+/* ------------------------------------------------------- banded level 2 */
+/* test/level2/sgbmv/exo_sgbmv.h:5-23, dgbmv likewise: y = beta y + alpha A x,
+ * A an M x N band (KL sub-, KU super-diagonals) in row-major band storage
+ * (row i holds columns i-KL .. i+KU); no Order / Trans argument */
+EXOBLAS_API void exo_sgbmv(const int M, const int N, const int KL, const int KU, const float alpha, const float *A,
+               const int lda, const float *X, const int incX, const float beta, float *Y, const int incY);
+EXOBLAS_API void exo_dgbmv(const int M, const int N, const int KL, const int KU, const double alpha, const double *A,
+               const int lda, const double *X, const int incX, const double beta, double *Y, const int incY);
+/* test/level2/ssbmv/exo_ssbmv.h:7-52: y = beta y + alpha A x, A symmetric with K off-diagonals */
+EXOBLAS_API void exo_ssbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K,
+               const float alpha, const float *A, const int lda, const float *X, const int incX, const float beta,
+               float *Y, const int incY);
+EXOBLAS_API void exo_dsbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K,
+               const double alpha, const double *A, const int lda, const double *X, const int incX, const double beta,
+               double *Y, const int incY);
+/* test/level2/stbmv/exo_stbmv.h: x = op(A) x, A triangular with K off-diagonals */
+EXOBLAS_API void exo_stbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
+               const int incX);
+EXOBLAS_API void exo_dtbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
+               const int incX);
+/* test/level2/stbsv/exo_stbsv.h: solve op(A) x = b in place, A triangular banded */
+EXOBLAS_API void exo_stbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
+               const int incX);
+EXOBLAS_API void exo_dtbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
+               const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
+               const int incX);
+
 /* ------------------------------------------------------------ level 3 --- */
 /* test/level3/gemm/exo_gemm_wrapper.h:9-28 (C *= beta, then C += alpha op(A) op(B)) */
 EXOBLAS_API void exo_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,

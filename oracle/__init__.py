@@ -91,6 +91,14 @@ SIGS = {
     "oracle_dsymm": ("v", "iiiiidpipidpi"),
     "oracle_ssyrk": ("v", "iiiiifpifpi"),
     "oracle_dsyrk": ("v", "iiiiidpidpi"),
+    "oracle_sgbmv": ("v", "iiiifpipifpi"),
+    "oracle_dgbmv": ("v", "iiiidpipidpi"),
+    "oracle_ssbmv": ("v", "iiiifpipifpi"),
+    "oracle_dsbmv": ("v", "iiiidpipidpi"),
+    "oracle_stbmv": ("v", "iiiiiipipi"),
+    "oracle_dtbmv": ("v", "iiiiiipipi"),
+    "oracle_stbsv": ("v", "iiiiiipipi"),
+    "oracle_dtbsv": ("v", "iiiiiipipi"),
     "oracle_ssyr2k": ("v", "iiiiifpipifpi"),
     "oracle_dsyr2k": ("v", "iiiiidpipidpi"),
     "oracle_strmm": ("v", "iiiiiiifpipi"),

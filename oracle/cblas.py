@@ -36,6 +36,10 @@ SIGS = {
     "ssymm": ("v", "iiiiifpipifpi"), "dsymm": ("v", "iiiiidpipidpi"),
     "ssyrk": ("v", "iiiiifpifpi"), "dsyrk": ("v", "iiiiidpidpi"),
     "ssyr2k": ("v", "iiiiifpipifpi"), "dsyr2k": ("v", "iiiiidpipidpi"),
+    "ssbmv": ("v", "iiiifpipifpi"), "dsbmv": ("v", "iiiidpipidpi"),
+    "sgbmv": ("v", "iiiiiifpipifpi"), "dgbmv": ("v", "iiiiiidpipidpi"),
+    "stbmv": ("v", "iiiiiipipi"), "dtbmv": ("v", "iiiiiipipi"),
+    "stbsv": ("v", "iiiiiipipi"), "dtbsv": ("v", "iiiiiipipi"),
     "strmm": ("v", "iiiiiiifpipi"), "dtrmm": ("v", "iiiiiiidpipi"),
 }
 

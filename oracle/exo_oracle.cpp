@@ -10,7 +10,7 @@
 // Each function cites the reference file:line it follows.  Sources:
 //   src/level1/{asum,axpy,dot,dsdot,exo_copy,rot,rotm,scal,swap}.py
 //   src/level2/{gemv,ger,symv,syr,syr2,trmv,trsv}.py
-//   src/level3/{gemm,symm,syrk,syr2k,trmm,mscal}.py
+//   src/level3/{gemm,symm,syrk,syr2k,trmm,mscal}.py, src/level2/{gbmv,sbmv,tbmv,tbsv}.py
 //   test/level*/<op>/exo_<op>_wrapper.h, test/level1/sdsdot/exo_sdsdot.h
 //
 // The reference raises a C++ exception when Order != RowMajor.  The oracle
@@ -575,6 +575,203 @@ void syrk_wrap(int order, int Uplo, int Trans, int N, int K, T alpha,
   syrk_rows<T>(Uplo, Trans, 0, N, N, K, alpha, a, c);
 }
 
+// ------------------------------------------------------- banded level 2 --
+// Vec<T>: element i at p[i * inc] (the wrapper has already rebased p).
+
+// src/level2/gbmv.py:12-50 (the proc leaves `result` unset for rows below
+// the band's last column; here it is 0, so y[i] = beta y[i] as in CBLAS)
+template <typename T>
+void gbmv_proc(long m, long n, long kl, long ku, T alpha, T beta, Mat<T> a, const T *x, long incx, T *y, long incy) {
+  for (long i = 0; i < m; ++i) {
+    T result = 0;
+    if (i - kl >= 0) {
+      if (i + ku < n) {
+        for (long j = 0; j < kl + ku + 1; ++j) result += a(i, j) * x[(i + (j - kl)) * incx];
+      } else if (kl + n - i > 0) {
+        for (long j = 0; j < kl + n - i; ++j) result += a(i, j) * x[(i + (j - kl)) * incx];
+      }
+    } else {
+      if (i + ku < n) {
+        for (long j = 0; j < i + ku + 1; ++j) result += a(i, kl - i + j) * x[j * incx];
+      } else {
+        for (long j = 0; j < n; ++j) result += a(i, kl - i + j) * x[j * incx];
+      }
+    }
+    y[i * incy] = beta * y[i * incy] + alpha * result;
+  }
+}
+
+// test/level2/sgbmv/exo_sgbmv.h:5-23.  That wrapper does not rebase negative
+// increments (it would read before X); here they follow the CBLAS rule.
+template <typename T>
+void gbmv_wrap(int M, int N, int KL, int KU, T alpha, const T *A, int lda, const T *X, int incX, T beta, T *Y,
+               int incY) {
+  g_status = 0;
+  if (incX < 0) X = X + long(1 - N) * incX;
+  if (incY < 0) Y = Y + long(1 - M) * incY;
+  gbmv_proc<T>(M, N, KL, KU, alpha, beta, Mat<T>{const_cast<T *>(A), lda}, X, incX, Y, incY);
+}
+
+// src/level2/sbmv.py:8-44 and test/level2/ssbmv/exo_ssbmv.h:7-52
+template <typename T>
+void sbmv_wrap(int order, int Uplo, int N, int K, T alpha, const T *A, int lda, const T *X, int incX, T beta, T *Y,
+               int incY) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  if (incX < 0) X = X + long(1 - N) * incX;
+  if (incY < 0) Y = Y + long(1 - N) * incY;
+  Mat<T> a{const_cast<T *>(A), lda};
+  auto x = [&](long i) -> T { return X[i * incX]; };
+  auto y = [&](long i) -> T & { return Y[i * incY]; };
+  if (beta != T(1))
+    for (long i = 0; i < N; ++i) y(i) = beta * y(i);
+  for (long i = 0; i < N; ++i) {
+    const T temp = alpha * x(i);
+    T dot = 0;
+    if (Uplo == kUpper) {
+      for (long j = 0; j < K; ++j)
+        if (i + j + 1 < N) {
+          y(i + j + 1) += temp * a(i, j + 1);
+          dot += a(i, j + 1) * x(i + j + 1);
+        }
+      y(i) += temp * a(i, 0) + alpha * dot;
+    } else {
+      for (long j = 0; j < K; ++j)
+        if (i - j - 1 >= 0) {
+          y(i - j - 1) += temp * a(i, K - j - 1);
+          dot += a(i, K - j - 1) * x(i - j - 1);
+        }
+      y(i) += temp * a(i, K) + alpha * dot;
+    }
+  }
+}
+
+// src/level2/tbmv.py:9-120 (the four procs in their loop order)
+template <typename T>
+void tbmv_proc(bool upper, bool trans, bool unit, long n, long k, Mat<T> a, T *X, long inc) {
+  auto x = [&](long i) -> T & { return X[i * inc]; };
+  if (!trans) {
+    if (upper) {
+      for (long i = 0; i < n - k; ++i) {
+        T dot = unit ? x(i) : x(i) * a(i, 0);
+        for (long j = 0; j < k; ++j) dot += a(i, j + 1) * x(i + j + 1);
+        x(i) = dot;
+      }
+      for (long i = 0; i < k; ++i) {
+        const long r = n - k + i;
+        T dot = unit ? x(r) : x(r) * a(r, 0);
+        for (long j = 0; j < k - i - 1; ++j) dot += a(r, j + 1) * x(r + j + 1);
+        x(r) = dot;
+      }
+    } else {
+      for (long i = 0; i < n - k; ++i) {
+        const long r = n - i - 1;
+        T dot = 0;
+        for (long j = 0; j < k; ++j) dot += a(r, k - j - 1) * x(r - j - 1);
+        dot += unit ? x(r) : x(r) * a(r, k);
+        x(r) = dot;
+      }
+      for (long i = 0; i < k; ++i) {
+        const long r = k - i - 1;
+        T dot = 0;
+        for (long j = 0; j < k - i - 1; ++j) dot += a(r, k - j - 1) * x(r - j - 1);
+        dot += unit ? x(r) : x(r) * a(r, k);
+        x(r) = dot;
+      }
+    }
+    return;
+  }
+  std::vector<T> res(size_t(n), T(0));
+  if (upper) {
+    for (long i = 0; i < n - k; ++i) {
+      res[i] += unit ? x(i) : x(i) * a(i, 0);
+      for (long j = 0; j < k; ++j) res[i + j + 1] += a(i, j + 1) * x(i);
+    }
+    for (long i = 0; i < k; ++i) {
+      const long r = n - k + i;
+      res[r] += unit ? x(r) : x(r) * a(r, 0);
+      for (long j = 0; j < k - i - 1; ++j) res[r + j + 1] += a(r, j + 1) * x(r);
+    }
+  } else {
+    for (long i = 0; i < n - k; ++i) {
+      const long r = n - i - 1;
+      for (long j = 0; j < k; ++j) res[r - j - 1] += a(r, k - j - 1) * x(r);
+      res[r] += unit ? x(r) : x(r) * a(r, k);
+    }
+    for (long i = 0; i < k; ++i) {
+      const long r = k - i - 1;
+      for (long j = 0; j < k - i - 1; ++j) res[r - j - 1] += a(r, k - j - 1) * x(r);
+      res[r] += unit ? x(r) : x(r) * a(r, k);
+    }
+  }
+  for (long i = 0; i < n; ++i) x(i) = res[i];
+}
+
+// src/level2/tbsv.py:9-120 (the four procs in their loop order)
+template <typename T>
+void tbsv_proc(bool upper, bool trans, bool unit, long n, long k, Mat<T> a, T *X, long inc) {
+  auto x = [&](long i) -> T & { return X[i * inc]; };
+  if (!trans && upper) {
+    for (long i = 0; i < k; ++i) {
+      const long r = n - i - 1;
+      const T pivot = unit ? T(1) : a(r, 0);
+      T dot = 0;
+      for (long j = 0; j < i; ++j) dot += a(r, j + 1) * x(n - i + j);
+      x(r) = (x(r) - dot) / pivot;
+    }
+    for (long i = 0; i < n - k; ++i) {
+      const long r = n - (k + i) - 1;
+      const T pivot = unit ? T(1) : a(r, 0);
+      T dot = 0;
+      for (long j = 0; j < k; ++j) dot += a(r, j + 1) * x(n - (k + i) + j);
+      x(r) = (x(r) - dot) / pivot;
+    }
+  } else if (!trans) {
+    for (long i = 0; i < k; ++i) {
+      T dot = 0;
+      for (long j = 0; j < i; ++j) dot += a(i, k - j - 1) * x(i - j - 1);
+      const T pivot = unit ? T(1) : a(i, k);
+      x(i) = (x(i) - dot) / pivot;
+    }
+    for (long i = 0; i < n - k; ++i) {
+      T dot = 0;
+      for (long j = 0; j < k; ++j) dot += a(i + k, k - j - 1) * x(i + k - j - 1);
+      const T pivot = unit ? T(1) : a(i + k, k);
+      x(i + k) = (x(i + k) - dot) / pivot;
+    }
+  } else if (upper) {
+    for (long i = 0; i < n; ++i) {
+      T dot = 0;
+      for (long j = 0; j < k; ++j)
+        if (i - j - 1 >= 0) dot += a(i - j - 1, j + 1) * x(i - j - 1);
+      const T pivot = unit ? T(1) : a(i, 0);
+      x(i) = (x(i) - dot) / pivot;
+    }
+  } else {
+    for (long i = 0; i < n; ++i) {
+      const T pivot = unit ? T(1) : a(n - i - 1, k);
+      T dot = 0;
+      for (long j = 0; j < k; ++j)
+        if (n - i + j < n) dot += a(n - i + j, k - j - 1) * x(n - i + j);
+      x(n - i - 1) = (x(n - i - 1) - dot) / pivot;
+    }
+  }
+}
+
+// test/level2/stbmv/exo_stbmv.h, test/level2/stbsv/exo_stbsv.h
+template <typename T>
+void tb_wrap(bool solve, int order, int Uplo, int TransA, int Diag, int N, int K, const T *A, int lda, T *X,
+             int incX) {
+  g_status = 0;
+  if (!row_major_or_fail(order)) return;
+  if (incX < 0) X = X + long(1 - N) * incX;
+  Mat<T> a{const_cast<T *>(A), lda};
+  if (solve)
+    tbsv_proc<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, N, K, a, X, incX);
+  else
+    tbmv_proc<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, N, K, a, X, incX);
+}
+
 // src/level3/syr2k.py:14-37: C[i,j] += alpha * (A[i,k] B[j,k] + B[i,k] A[j,k])
 // over the stored triangle (NoTrans), with A^T / B^T read as AT[k,i] (Trans)
 template <typename T>
@@ -797,6 +994,14 @@ ORACLE_API void oracle_dsymm(int order, int Side, int Uplo, int M, int N, double
 ORACLE_API void oracle_ssyrk(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, float beta, float *C, int ldc) { syrk_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
 ORACLE_API void oracle_dsyrk(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, double beta, double *C, int ldc) { syrk_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
 
+ORACLE_API void oracle_sgbmv(int M, int N, int KL, int KU, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { gbmv_wrap<float>(M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dgbmv(int M, int N, int KL, int KU, double alpha, const double *A, int lda, const double *X, int incX, double beta, double *Y, int incY) { gbmv_wrap<double>(M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_ssbmv(int order, int Uplo, int N, int K, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { sbmv_wrap<float>(order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dsbmv(int order, int Uplo, int N, int K, double alpha, const double *A, int lda, const double *X, int incX, double beta, double *Y, int incY) { sbmv_wrap<double>(order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_stbmv(int order, int Uplo, int TransA, int Diag, int N, int K, const float *A, int lda, float *X, int incX) { tb_wrap<float>(false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
+ORACLE_API void oracle_dtbmv(int order, int Uplo, int TransA, int Diag, int N, int K, const double *A, int lda, double *X, int incX) { tb_wrap<double>(false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
+ORACLE_API void oracle_stbsv(int order, int Uplo, int TransA, int Diag, int N, int K, const float *A, int lda, float *X, int incX) { tb_wrap<float>(true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
+ORACLE_API void oracle_dtbsv(int order, int Uplo, int TransA, int Diag, int N, int K, const double *A, int lda, double *X, int incX) { tb_wrap<double>(true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
 ORACLE_API void oracle_ssyr2k(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, const float *B, int ldb, float beta, float *C, int ldc) { syr2k_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
 ORACLE_API void oracle_dsyr2k(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { syr2k_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
 ORACLE_API void oracle_strmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, float alpha, const float *A, int lda, float *B, int ldb) { trmm_wrap<float>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }

@@ -264,3 +264,51 @@ def trmm_cases(Ms=(4, 101, 321), Ns=(8, 15, 564), alphas=(0.0, 1.0, 1.4), ldds=(
         yield Case("strmm", [ROW, LEFT, u, t, d, m, n, al, A, lda, B, ldb], [10], nred=m + 1,
                    label=f"m={m} n={n} u={u} t={t} d={d} alpha={al} lda={lda} ldb={ldb}")
 
+
+# ------------------------------------------------------------ banded level 2 --
+
+def gbmv_cases(p, sizes=((2, 2, 1, 1), (15, 20, 0, 5), (256, 256, 255, 255)), incs=((1, 1),)):
+    """test/level2/sgbmv/correctness.cpp:36-50 (alpha = beta = 1.2, lda = KL + KU + 1)"""
+    for (m, n, kl, ku), (ix, iy) in itertools.product(sizes, incs):
+        g = rng(_seed("gbmv", p, m, n, kl, ku, ix, iy))
+        lda = kl + ku + 1
+        A, x, y = mat(g, m, lda, DT[p]), buf(g, n, ix, DT[p]), buf(g, m, iy, DT[p])
+        yield Case(p + "gbmv", [m, n, kl, ku, 1.2, A, lda, x, ix, 1.2, y, iy], [10], nred=kl + ku + 2,
+                   label=f"m={m} n={n} kl={kl} ku={ku} incx={ix} incy={iy}", extra={"tol": 1e-3})
+
+
+def sbmv_cases(p, Ns=(2, 100, 321), Ks=(0, 1, 50)):
+    """test/level2/ssbmv/correctness.cpp:39-70 (alpha 2.4; beta 0, 1; incX 1, 3;
+    incY 1, -2; lda = K + 1 + {0, 3}, plus K = N - 1 with lda = N + {0, 3})"""
+    for u, n, ldd, ix, be, iy in itertools.product((UP, LO), Ns, (0, 3), (1, 3), (0.0, 1.0), (1, -2)):
+        for k, lda in [(k, k + 1 + ldd) for k in Ks if k <= n - 1] + [(n - 1, n + ldd)]:
+            g = rng(_seed("sbmv", p, u, n, k, ldd, ix, be, iy))
+            A, x, y = mat(g, n, lda, DT[p]), buf(g, n, ix, DT[p]), buf(g, n, iy, DT[p])
+            yield Case(p + "sbmv", [ROW, u, n, k, 2.4, A, lda, x, ix, be, y, iy], [10], nred=2 * k + 2,
+                       label=f"u={u} n={n} k={k} lda={lda} incx={ix} beta={be} incy={iy}")
+
+
+def tbmv_cases(p, Ns=(2, 100, 321), Ks=(0, 1, 6)):
+    """test/level2/stbmv/correctness.cpp:37-64 (lda = K + 1 + {0, 3}, incX 1, 3,
+    plus K = N - 1 with lda = N + {0, 3})"""
+    for n, u, t, d, ldd, ix in itertools.product(Ns, (UP, LO), (NT, TR), (NU, UN), (0, 3), (1, 3)):
+        for k, lda in [(k, k + 1 + ldd) for k in Ks if k <= n - 1] + [(n - 1, n + ldd)]:
+            g = rng(_seed("tbmv", p, n, u, t, d, k, ldd, ix))
+            A, x = mat(g, n, lda, DT[p]), buf(g, n, ix, DT[p])
+            yield Case(p + "tbmv", [ROW, u, t, d, n, k, A, lda, x, ix], [8], nred=k + 1,
+                       label=f"n={n} u={u} t={t} d={d} k={k} lda={lda} incx={ix}")
+
+
+def tbsv_cases(p, Ns=(2, 100, 321), Ks=(0, 1, 2, 10, 60)):
+    """test/level2/stbsv/correctness.cpp:11-75: A uniform[-1, 1) / 1000 with the
+    diagonal entries set to 2; lda = K + 1 (the reference's loop also repeats
+    K = N - 1 with lda = N + {0, 3} per K)"""
+    for n, u, t, d, ldd, ix in itertools.product(Ns, (UP, LO), (NT, TR), (UN, NU), (0, 3), (1, 3)):
+        for k, lda in [(k, k + 1 + ldd) for k in Ks if k <= n - 1] + [(n - 1, n + ldd)]:
+            g = rng(_seed("tbsv", p, n, u, t, d, k, ldd, ix))
+            A = (g.uniform(-1.0, 1.0, n * lda) / 1000).astype(DT[p])
+            A.reshape(n, lda)[:, 0 if u == UP else k] = 2
+            x = buf(g, n, ix, DT[p])
+            yield Case(p + "tbsv", [ROW, u, t, d, n, k, A, lda, x, ix], [8], nred=k + 1,
+                       label=f"n={n} u={u} t={t} d={d} k={k} lda={lda} incx={ix}")
+

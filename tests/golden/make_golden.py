@@ -54,6 +54,11 @@ def families():
     f["syrk"] = subset((c for p in "sd" for c in C.syrk_cases(p, dims=(1, 7, 32, 64))), 5)
     f["syr2k"] = subset((c for p in "sd" for c in C.syr2k_cases(p, dims=(1, 7, 32))), 7)
     f["trmm"] = subset(C.trmm_cases(Ms=(4, 33), Ns=(8, 15)), 3)
+    f["gbmv"] = subset((c for p in "sd" for c in C.gbmv_cases(p, sizes=((2, 2, 1, 1), (15, 20, 0, 5), (40, 33, 7, 3)),
+                                                            incs=((1, 1), (2, -3)))), 1)
+    f["sbmv"] = subset((c for p in "sd" for c in C.sbmv_cases(p, Ns=(2, 100), Ks=(0, 1, 50))), 5)
+    f["tbmv"] = subset((c for p in "sd" for c in C.tbmv_cases(p, Ns=(2, 100))), 5)
+    f["tbsv"] = subset((c for p in "sd" for c in C.tbsv_cases(p, Ns=(2, 100))), 5)
     return f
 
 
