@@ -28,6 +28,10 @@ L1 = {
     # name: (restype, argtypes)  -- pointers are 'p'
     "exo_sasum": ("f", "ipi"),
     "exo_dasum": ("d", "ipi"),
+    "exo_snrm2": ("f", "ipi"),
+    "exo_dnrm2": ("d", "ipi"),
+    "exo_isamax": ("z", "ipi"),
+    "exo_idamax": ("z", "ipi"),
     "exo_saxpy": ("v", "ifpipi"),
     "exo_daxpy": ("v", "idpipi"),
     "exo_sdot": ("f", "ipipi"),

@@ -46,6 +46,37 @@ static T asum_entry(const char *fn, int N, const T *X, int incX) {
   return r;
 }
 
+// nrm2 / iamax (no reference counterpart; reference BLAS semantics).  nrm2:
+// 0 for N < 1, any increment (negative walks backwards, 0 repeats x[0]);
+// iamax: 0 for N < 1 or incX < 1.
+template <typename T>
+static T nrm2_entry(const char *fn, int N, const T *X, int incX) {
+  T r = 0;
+  guarded(fn, [&] {
+    if (N < 1) return;
+    X = rebase(X, N, incX);
+    Stager st;
+    const T *dx = st.vec(X, N, incX, false);
+    T *res = static_cast<T *>(result_slot());
+    l1::nrm2<T>(N, dx, incX, res);
+    r = fetch_result<T>(res);
+  });
+  return r;
+}
+template <typename T>
+static size_t iamax_entry(const char *fn, int N, const T *X, int incX) {
+  size_t r = 0;
+  guarded(fn, [&] {
+    if (N < 1 || incX < 1) return;
+    Stager st;
+    const T *dx = st.vec(X, N, incX, false);
+    size_t *res = static_cast<size_t *>(result_slot());
+    l1::iamax<T>(N, dx, incX, res);
+    r = fetch_result<size_t>(res);
+  });
+  return r;
+}
+
 // test/level1/axpy/exo_axpy_wrapper.h:5-34
 template <typename T>
 static void axpy_entry(const char *fn, int N, T alpha, const T *X, int incX, T *Y, int incY) {
@@ -229,6 +260,14 @@ using namespace exb;
 extern "C" {
 
 float exo_sasum(const int N, const float *X, const int incX) { return asum_entry<float>("exo_sasum", N, X, incX); }
+float exo_snrm2(const int N, const float *X, const int incX) { return nrm2_entry<float>("exo_snrm2", N, X, incX); }
+double exo_dnrm2(const int N, const double *X, const int incX) { return nrm2_entry<double>("exo_dnrm2", N, X, incX); }
+size_t exo_isamax(const int N, const float *X, const int incX) {
+  return iamax_entry<float>("exo_isamax", N, X, incX);
+}
+size_t exo_idamax(const int N, const double *X, const int incX) {
+  return iamax_entry<double>("exo_idamax", N, X, incX);
+}
 double exo_dasum(const int N, const double *X, const int incX) { return asum_entry<double>("exo_dasum", N, X, incX); }
 
 void exo_saxpy(const int N, const float alpha, const float *X, const int incX, float *Y, const int incY) {

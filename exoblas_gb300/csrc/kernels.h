@@ -29,6 +29,12 @@ void dot(long n, const T *x, long incx, const T *y, long incy, T *result);
 // result (double) = sum of double(x_i) * double(y_i); if sresult != nullptr
 // also writes float(result + sb) there (sdsdot)
 void dsdot(long n, const float *x, long incx, const float *y, long incy, double *result, float sb, float *sresult);
+// sqrt(sum x_i^2) without overflow or underflow; 0-based index of the first
+// largest |x_i| (device results)
+template <typename T>
+void nrm2(long n, const T *x, long incx, T *result);
+template <typename T>
+void iamax(long n, const T *x, long incx, size_t *result);
 }  // namespace l1
 
 namespace l2 {

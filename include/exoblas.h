@@ -110,6 +110,15 @@ EXOBLAS_API void exoblas_staged_bytes(unsigned long long *h2d, unsigned long lon
 /* test/level1/asum/exo_asum_wrapper.h:5-23 (incX < 0 returns 0) */
 EXOBLAS_API float exo_sasum(const int N, const float *X, const int incX);
 EXOBLAS_API double exo_dasum(const int N, const double *X, const int incX);
+/* nrm2 and i?amax: standard level-1 routines the reference lacks
+ * (README.md:15), with reference BLAS semantics.  nrm2: free of overflow and
+ * underflow, 0 for N < 1, any increment (negative walks the vector
+ * backwards, 0 repeats X[0]); i?amax: 0 for N < 1 or incX < 1, else the
+ * 0-based index (as cblas_i?amax) of the first element of largest magnitude */
+EXOBLAS_API float exo_snrm2(const int N, const float *X, const int incX);
+EXOBLAS_API double exo_dnrm2(const int N, const double *X, const int incX);
+EXOBLAS_API size_t exo_isamax(const int N, const float *X, const int incX);
+EXOBLAS_API size_t exo_idamax(const int N, const double *X, const int incX);
 /* test/level1/axpy/exo_axpy_wrapper.h:5-34 (alpha == 0 returns) */
 EXOBLAS_API void exo_saxpy(const int N, const float alpha, const float *X, const int incX, float *Y, const int incY);
 EXOBLAS_API void exo_daxpy(const int N, const double alpha, const double *X, const int incX, double *Y, const int incY);

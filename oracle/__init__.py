@@ -91,6 +91,10 @@ SIGS = {
     "oracle_dsymm": ("v", "iiiiidpipidpi"),
     "oracle_ssyrk": ("v", "iiiiifpifpi"),
     "oracle_dsyrk": ("v", "iiiiidpidpi"),
+    "oracle_snrm2": ("f", "ipi"),
+    "oracle_dnrm2": ("d", "ipi"),
+    "oracle_isamax": ("l", "ipi"),
+    "oracle_idamax": ("l", "ipi"),
     "oracle_sgbmv": ("v", "iiiifpipifpi"),
     "oracle_dgbmv": ("v", "iiiidpipidpi"),
     "oracle_ssbmv": ("v", "iiiifpipifpi"),

@@ -13,10 +13,12 @@ import ctypes as C
 import glob
 import os
 
-_T = {"i": C.c_int, "f": C.c_float, "d": C.c_double, "p": C.c_void_p, "v": None}
+_T = {"i": C.c_int, "f": C.c_float, "d": C.c_double, "p": C.c_void_p, "z": C.c_size_t, "v": None}
 
 SIGS = {
     "sasum": ("f", "ipi"), "dasum": ("d", "ipi"),
+    "snrm2": ("f", "ipi"), "dnrm2": ("d", "ipi"),
+    "isamax": ("z", "ipi"), "idamax": ("z", "ipi"),
     "saxpy": ("v", "ifpipi"), "daxpy": ("v", "idpipi"),
     "sdot": ("f", "ipipi"), "ddot": ("d", "ipipi"),
     "dsdot": ("d", "ipipi"), "sdsdot": ("f", "ifpipi"),

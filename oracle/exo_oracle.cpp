@@ -575,6 +575,50 @@ void syrk_wrap(int order, int Uplo, int Trans, int N, int K, T alpha,
   syrk_rows<T>(Uplo, Trans, 0, N, N, K, alpha, a, c);
 }
 
+// --------------------------------------------------------- nrm2, iamax --
+// No reference counterpart (README.md:15).  nrm2: the two-pass scaled sum
+// of squares (scale = max |x_i|, then scale * sqrt(sum (x_i / scale)^2)),
+// free of overflow and underflow, over any increment (a negative one walks
+// the vector backwards, 0 repeats x[0]) as in reference BLAS 3.10 and
+// OpenBLAS; iamax: the reference BLAS loop (0 for N < 1 or incX < 1; start
+// from |x[0]|, take an element only when strictly larger), 0-based.
+template <typename T>
+T nrm2_ref(int N, const T *X, int incX) {
+  g_status = 0;
+  if (N < 1) return T(0);
+  if (incX < 0) X = X + long(1 - N) * incX;  // any increment, as the current reference BLAS
+  double scale = 0;
+  bool nan = false;
+  for (long i = 0; i < N; ++i) {
+    const double v = std::fabs(double(X[i * incX]));
+    if (v != v) nan = true;
+    if (v > scale) scale = v;
+  }
+  if (nan) return T(NAN);
+  if (scale == 0 || std::isinf(scale)) return T(scale);
+  double ss = 0;
+  for (long i = 0; i < N; ++i) {
+    const double v = double(X[i * incX]) / scale;
+    ss += v * v;
+  }
+  return T(scale * std::sqrt(ss));
+}
+template <typename T>
+long iamax_ref(int N, const T *X, int incX) {
+  g_status = 0;
+  if (N < 1 || incX < 1) return 0;
+  long best = 0;
+  T mx = std::fabs(X[0]);
+  for (long i = 1; i < N; ++i) {
+    const T v = std::fabs(X[i * incX]);
+    if (v > mx) {
+      mx = v;
+      best = i;
+    }
+  }
+  return best;
+}
+
 // ------------------------------------------------------- banded level 2 --
 // Vec<T>: element i at p[i * inc] (the wrapper has already rebased p).
 
@@ -994,6 +1038,10 @@ ORACLE_API void oracle_dsymm(int order, int Side, int Uplo, int M, int N, double
 ORACLE_API void oracle_ssyrk(int order, int Uplo, int Trans, int N, int K, float alpha, const float *A, int lda, float beta, float *C, int ldc) { syrk_wrap<float>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
 ORACLE_API void oracle_dsyrk(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, double beta, double *C, int ldc) { syrk_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
 
+ORACLE_API float oracle_snrm2(int N, const float *X, int incX) { return nrm2_ref<float>(N, X, incX); }
+ORACLE_API double oracle_dnrm2(int N, const double *X, int incX) { return nrm2_ref<double>(N, X, incX); }
+ORACLE_API long oracle_isamax(int N, const float *X, int incX) { return iamax_ref<float>(N, X, incX); }
+ORACLE_API long oracle_idamax(int N, const double *X, int incX) { return iamax_ref<double>(N, X, incX); }
 ORACLE_API void oracle_sgbmv(int M, int N, int KL, int KU, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { gbmv_wrap<float>(M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY); }
 ORACLE_API void oracle_dgbmv(int M, int N, int KL, int KU, double alpha, const double *A, int lda, const double *X, int incX, double beta, double *Y, int incY) { gbmv_wrap<double>(M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY); }
 ORACLE_API void oracle_ssbmv(int order, int Uplo, int N, int K, float alpha, const float *A, int lda, const float *X, int incX, float beta, float *Y, int incY) { sbmv_wrap<float>(order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY); }

@@ -312,3 +312,32 @@ def tbsv_cases(p, Ns=(2, 100, 321), Ks=(0, 1, 2, 10, 60)):
             yield Case(p + "tbsv", [ROW, u, t, d, n, k, A, lda, x, ix], [8], nred=k + 1,
                        label=f"n={n} u={u} t={t} d={d} k={k} lda={lda} incx={ix}")
 
+
+# ---------------------------------------------------------------- nrm2, iamax --
+
+def nrm2_cases(p, Ns=(1, 2, 7, 100, 1000, 20000), incs=(1, 3, -1, 0), scales=(1.0, 1e200, 1e-200)):
+    """nrm2 has no reference test (README.md:15); sizes and increments follow
+    the level-1 grids, plus FP64 magnitudes whose squares overflow or
+    underflow, and non-positive increments (result 0)."""
+    for n, inc, sc in itertools.product(Ns, incs, scales):
+        if p == "s" and sc != 1.0:
+            continue
+        g = rng(_seed("nrm2", p, n, inc, sc))
+        x = (buf(g, n, max(abs(inc), 1), np.float64) * sc).astype(DT[p])
+        yield Case(p + "nrm2", [n, x, inc], [], scalar=True, nred=n, label=f"n={n} inc={inc} scale={sc:g}")
+
+
+def iamax_cases(p, Ns=(1, 2, 7, 100, 1000, 20000), incs=(1, 3, -1, 0)):
+    """i?amax: first index of the largest magnitude; ties planted so the
+    first-index rule is exercised."""
+    for n, inc, tie in itertools.product(Ns, incs, (False, True)):
+        g = rng(_seed("iamax", p, n, inc, tie))
+        x = buf(g, n, max(abs(inc), 1), DT[p])
+        if tie and n > 2:
+            step = max(abs(inc), 1)
+            hi = DT[p](1.5)
+            for pos in sorted(g.choice(n, 3, replace=False)):
+                x[pos * step] = hi if pos % 2 else -hi
+        yield Case(p[0] if False else ("i" + p + "amax"), [n, x, inc], [], scalar=True, exact=True, nred=n,
+                   label=f"n={n} inc={inc} tie={tie}")
+

@@ -59,6 +59,8 @@ def families():
     f["sbmv"] = subset((c for p in "sd" for c in C.sbmv_cases(p, Ns=(2, 100), Ks=(0, 1, 50))), 5)
     f["tbmv"] = subset((c for p in "sd" for c in C.tbmv_cases(p, Ns=(2, 100))), 5)
     f["tbsv"] = subset((c for p in "sd" for c in C.tbsv_cases(p, Ns=(2, 100))), 5)
+    f["nrm2"] = subset((c for p in "sd" for c in C.nrm2_cases(p, Ns=(1, 2, 7, 100, 1000))), 1)
+    f["iamax"] = subset((c for p in "sd" for c in C.iamax_cases(p, Ns=(1, 2, 7, 100, 1000))), 1)
     return f
 
 

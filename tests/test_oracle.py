@@ -25,10 +25,12 @@ def fixture(name, i):
 
 def check_against(case, got_r, got_args, exp_r, exp_out, what):
     if case.exact:
+        if case.scalar:
+            assert got_r == exp_r, f"{what}: {case} result {got_r} != {exp_r}"
         for j, e in exp_out.items():
             assert got_args[j].tobytes() == e.tobytes(), f"{what}: {case} output {j} not bit-exact"
         return
-    if case.op.endswith("trsv"):
+    if case.op.endswith("trsv") or case.op.endswith("tbsv"):
         for j, e in exp_out.items():
             assert_rel1pct(got_args[j], e, f"{what} {case}")
         return
