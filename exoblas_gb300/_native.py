@@ -109,6 +109,8 @@ EXTRA = {
     "exoblas_batch_plan_destroy": ("i", "p"),
     "exoblas_batch_tune": ("i", ""),
     "exoblas_batch_tile_config": ("i", "iii"),
+    "exoblas_set_column_major": ("i", "i"),
+    "exoblas_get_column_major": ("i", ""),
     "exoblas_server_create": ("i", "izzzp"),
     "exoblas_server_submit": ("i", "ppd"),
     "exoblas_server_now": ("d", ""),

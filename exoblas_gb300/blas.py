@@ -110,6 +110,12 @@ def get_precision() -> int:
     return _native.lib().exoblas_get_precision()
 
 
+def set_column_major(enable: bool) -> None:
+    """Accept CblasColMajor calls on this thread (rejected by default, as in
+    the reference)."""
+    _native.lib().exoblas_set_column_major(1 if enable else 0)
+
+
 def set_blocking(blocking: bool) -> None:
     _native.lib().exoblas_set_blocking(1 if blocking else 0)
     _check("exoblas_set_blocking")
@@ -166,6 +172,7 @@ __all__ = _EXO + [
     "ExoBlasError",
     "UnsupportedParameterException",
     "set_precision",
+    "set_column_major",
     "get_precision",
     "set_blocking",
     "set_stream",

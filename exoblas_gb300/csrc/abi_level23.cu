@@ -403,25 +403,43 @@ static void syr2k_entry(const char *fn, int Order, int Uplo, int Trans, int N, i
 }
 
 // test/level3/strmm/exo_strmm.h:7-58: Left only (the reference's Right
-// branches are empty); Diag is unit only when it equals CblasUnit.
+// branches are empty, so a row-major Right call leaves B unchanged); Diag is
+// unit only when it equals CblasUnit.  right_ok: the column-major mapping
+// of a Left call, B^T = alpha B^T op(A)^T, runs as a row-major Right call.
 template <typename T>
 static void trmm_entry(const char *fn, int Order, int Side, int Uplo, int TransA, int Diag, int M, int N, T alpha,
-                       const T *A, int lda, T *B, int ldb) {
+                       const T *A, int lda, T *B, int ldb, bool right_ok = false) {
   guarded(fn, [&] {
     row_major(Order);
-    if (Side != kLeft) return;
+    const bool left = Side == kLeft;
+    if (!left && !right_ok) return;
     nonneg(M, "M < 0");
     nonneg(N, "N < 0");
     if (M == 0 || N == 0) return;
-    ld_ok(lda, M, "lda < max(1, M)");
+    const long ka = left ? M : N;  // A is ka x ka
+    ld_ok(lda, ka, "lda < max(1, K)");
     ld_ok(ldb, N, "ldb < max(1, N)");
     Stager st;
-    const T *dA = st.mat(A, M, M, lda, false);
+    const T *dA = st.mat(A, ka, ka, lda, false);
     T *dB = st.mat(B, M, N, ldb, true);
-    l3::trmm_simt<T>(Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, M, N, alpha, dA, lda, dB, ldb);
+    l3::trmm_simt<T>(left, Uplo == kUpper, TransA != kNoTrans, Diag == kUnit, M, N, alpha, dA, lda, dB, ldb);
     st.finish();
   });
 }
+
+// Column-major calls, when enabled (exoblas_set_column_major), are the
+// row-major call on the transposed view of every operand: a column-major
+// M x N matrix with leading dimension ld is the row-major N x M matrix with
+// the same ld.  So gemm swaps (A, TransA) with (B, TransB) and M with N,
+// gemv flips Trans and swaps M, N, ger swaps (X, M) with (Y, N), and the
+// triangle of a symmetric or triangular operand changes sides: Uplo flips,
+// with Trans (trmv/trsv/tbmv/tbsv/syrk/syr2k) or Side (symm/trmm) as the
+// transposition requires.  By default a column-major call is rejected, as
+// in the reference (e.g. test/level3/gemm/exo_gemm_wrapper.h:15-17).
+static bool col_major(int order) { return order == kColMajor && column_major_enabled(); }
+static CBLAS_TRANSPOSE flip_t(int t) { return CBLAS_TRANSPOSE(t == kNoTrans ? kTrans : kNoTrans); }
+static CBLAS_UPLO flip_u(int u) { return CBLAS_UPLO(u == kUpper ? kLower : kUpper); }
+static CBLAS_SIDE flip_s(int s) { return CBLAS_SIDE(s == kLeft ? kRight : kLeft); }
 
 }  // namespace exb
 
@@ -432,96 +450,112 @@ extern "C" {
 void exo_sgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N,
                const float alpha, const float *A, const int lda, const float *X, const int incX, const float beta,
                float *Y, const int incY) {
+  if (col_major(order)) return gemv_entry<float>("exo_sgemv", kRowMajor, flip_t(TransA), N, M, alpha, A, lda, X, incX, beta, Y, incY);
   gemv_entry<float>("exo_sgemv", order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_dgemv(const enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE TransA, const int M, const int N,
                const double alpha, const double *A, const int lda, const double *X, const int incX, const double beta,
                double *Y, const int incY) {
+  if (col_major(order)) return gemv_entry<double>("exo_dgemv", kRowMajor, flip_t(TransA), N, M, alpha, A, lda, X, incX, beta, Y, incY);
   gemv_entry<double>("exo_dgemv", order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_sger(const enum CBLAS_ORDER order, const int M, const int N, const float alpha, const float *X,
               const int incX, const float *Y, const int incY, float *A, const int lda) {
-  (void)order;
+  if (col_major(order)) return ger_entry<float>("exo_sger", N, M, alpha, Y, incY, X, incX, A, lda);
   ger_entry<float>("exo_sger", M, N, alpha, X, incX, Y, incY, A, lda);
 }
 void exo_dger(const enum CBLAS_ORDER order, const int M, const int N, const double alpha, const double *X,
               const int incX, const double *Y, const int incY, double *A, const int lda) {
-  (void)order;
+  if (col_major(order)) return ger_entry<double>("exo_dger", N, M, alpha, Y, incY, X, incX, A, lda);
   ger_entry<double>("exo_dger", M, N, alpha, X, incX, Y, incY, A, lda);
 }
 void exo_ssymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
                const float *A, const int lda, const float *X, const int incX, const float beta, float *Y,
                const int incY) {
+  if (col_major(order)) return symv_entry<float>("exo_ssymv", kRowMajor, flip_u(Uplo), N, alpha, A, lda, X, incX, beta, Y, incY);
   symv_entry<float>("exo_ssymv", order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_dsymv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
                const double *A, const int lda, const double *X, const int incX, const double beta, double *Y,
                const int incY) {
+  if (col_major(order)) return symv_entry<double>("exo_dsymv", kRowMajor, flip_u(Uplo), N, alpha, A, lda, X, incX, beta, Y, incY);
   symv_entry<double>("exo_dsymv", order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_ssyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
               const float *X, const int incX, float *A, const int lda) {
+  if (col_major(order)) return syr_entry<float>("exo_ssyr", kRowMajor, flip_u(Uplo), N, alpha, X, incX, A, lda);
   syr_entry<float>("exo_ssyr", order, Uplo, N, alpha, X, incX, A, lda);
 }
 void exo_dsyr(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
               const double *X, const int incX, double *A, const int lda) {
+  if (col_major(order)) return syr_entry<double>("exo_dsyr", kRowMajor, flip_u(Uplo), N, alpha, X, incX, A, lda);
   syr_entry<double>("exo_dsyr", order, Uplo, N, alpha, X, incX, A, lda);
 }
 void exo_ssyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const float alpha,
                const float *X, const int incX, const float *Y, const int incY, float *A, const int lda) {
-  (void)order;
+  if (col_major(order)) return syr2_entry<float>("exo_ssyr2", flip_u(Uplo), N, alpha, X, incX, Y, incY, A, lda);
   syr2_entry<float>("exo_ssyr2", Uplo, N, alpha, X, incX, Y, incY, A, lda);
 }
 void exo_dsyr2(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const double alpha,
                const double *X, const int incX, const double *Y, const int incY, double *A, const int lda) {
-  (void)order;
+  if (col_major(order)) return syr2_entry<double>("exo_dsyr2", flip_u(Uplo), N, alpha, X, incX, Y, incY, A, lda);
   syr2_entry<double>("exo_dsyr2", Uplo, N, alpha, X, incX, Y, incY, A, lda);
 }
 void exo_strmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX) {
+  if (col_major(order)) return tr_entry<float, false>("exo_strmv", kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, A, lda, X, incX);
   tr_entry<float, false>("exo_strmv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
 }
 void exo_dtrmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX) {
+  if (col_major(order)) return tr_entry<double, false>("exo_dtrmv", kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, A, lda, X, incX);
   tr_entry<double, false>("exo_dtrmv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
 }
 void exo_strsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const float *A, const int lda, float *X, const int incX) {
+  if (col_major(order)) return tr_entry<float, true>("exo_strsv", kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, A, lda, X, incX);
   tr_entry<float, true>("exo_strsv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
 }
 void exo_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const double *A, const int lda, double *X, const int incX) {
+  if (col_major(order)) return tr_entry<double, true>("exo_dtrsv", kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, A, lda, X, incX);
   tr_entry<double, true>("exo_dtrsv", order, Uplo, TransA, Diag, N, A, lda, X, incX);
 }
 
 void exo_sgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
                const int M, const int N, const int K, const float alpha, const float *A, const int lda,
                const float *B, const int ldb, const float beta, float *C, const int ldc) {
+  if (col_major(Order)) return gemm_entry<float>("exo_sgemm", kRowMajor, TransB, TransA, N, M, K, alpha, B, ldb, A, lda, beta, C, ldc);
   gemm_entry<float>("exo_sgemm", Order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_dgemm(const enum CBLAS_ORDER Order, const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_TRANSPOSE TransB,
                const int M, const int N, const int K, const double alpha, const double *A, const int lda,
                const double *B, const int ldb, const double beta, double *C, const int ldc) {
+  if (col_major(Order)) return gemm_entry<double>("exo_dgemm", kRowMajor, TransB, TransA, N, M, K, alpha, B, ldb, A, lda, beta, C, ldc);
   gemm_entry<double>("exo_dgemm", Order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_ssymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
                const int N, const float alpha, const float *A, const int lda, const float *B, const int ldb,
                const float beta, float *C, const int ldc) {
+  if (col_major(Order)) return symm_entry<float>("exo_ssymm", kRowMajor, flip_s(Side), flip_u(Uplo), N, M, alpha, A, lda, B, ldb, beta, C, ldc);
   symm_entry<float>("exo_ssymm", Order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_dsymm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo, const int M,
                const int N, const double alpha, const double *A, const int lda, const double *B, const int ldb,
                const double beta, double *C, const int ldc) {
+  if (col_major(Order)) return symm_entry<double>("exo_dsymm", kRowMajor, flip_s(Side), flip_u(Uplo), N, M, alpha, A, lda, B, ldb, beta, C, ldc);
   symm_entry<double>("exo_dsymm", Order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_ssyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
                const int N, const int K, const float alpha, const float *A, const int lda, const float beta, float *C,
                const int ldc) {
+  if (col_major(Order)) return syrk_entry<float>("exo_ssyrk", kRowMajor, flip_u(Uplo), flip_t(Trans), N, K, alpha, A, lda, beta, C, ldc);
   syrk_entry<float>("exo_ssyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
 }
 void exo_dsyrk(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
                const int N, const int K, const double alpha, const double *A, const int lda, const double beta,
                double *C, const int ldc) {
+  if (col_major(Order)) return syrk_entry<double>("exo_dsyrk", kRowMajor, flip_u(Uplo), flip_t(Trans), N, K, alpha, A, lda, beta, C, ldc);
   syrk_entry<double>("exo_dsyrk", Order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc);
 }
 void exo_sgbmv(const int M, const int N, const int KL, const int KU, const float alpha, const float *A,
@@ -535,46 +569,55 @@ void exo_dgbmv(const int M, const int N, const int KL, const int KU, const doubl
 void exo_ssbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K, const float alpha,
                const float *A, const int lda, const float *X, const int incX, const float beta, float *Y,
                const int incY) {
+  if (col_major(order)) return sbmv_entry<float>("exo_ssbmv", kRowMajor, flip_u(Uplo), N, K, alpha, A, lda, X, incX, beta, Y, incY);
   sbmv_entry<float>("exo_ssbmv", order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_dsbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const int N, const int K, const double alpha,
                const double *A, const int lda, const double *X, const int incX, const double beta, double *Y,
                const int incY) {
+  if (col_major(order)) return sbmv_entry<double>("exo_dsbmv", kRowMajor, flip_u(Uplo), N, K, alpha, A, lda, X, incX, beta, Y, incY);
   sbmv_entry<double>("exo_dsbmv", order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY);
 }
 void exo_stbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
                const int incX) {
+  if (col_major(order)) return tb_entry<float>("exo_stbmv", false, kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, K, A, lda, X, incX);
   tb_entry<float>("exo_stbmv", false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
 }
 void exo_dtbmv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
                const int incX) {
+  if (col_major(order)) return tb_entry<double>("exo_dtbmv", false, kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, K, A, lda, X, incX);
   tb_entry<double>("exo_dtbmv", false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
 }
 void exo_stbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const int K, const float *A, const int lda, float *X,
                const int incX) {
+  if (col_major(order)) return tb_entry<float>("exo_stbsv", true, kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, K, A, lda, X, incX);
   tb_entry<float>("exo_stbsv", true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
 }
 void exo_dtbsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE TransA,
                const enum CBLAS_DIAG Diag, const int N, const int K, const double *A, const int lda, double *X,
                const int incX) {
+  if (col_major(order)) return tb_entry<double>("exo_dtbsv", true, kRowMajor, flip_u(Uplo), flip_t(TransA), Diag, N, K, A, lda, X, incX);
   tb_entry<double>("exo_dtbsv", true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX);
 }
 void exo_ssyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
                 const int N, const int K, const float alpha, const float *A, const int lda, const float *B,
                 const int ldb, const float beta, float *C, const int ldc) {
+  if (col_major(Order)) return syr2k_entry<float>("exo_ssyr2k", kRowMajor, flip_u(Uplo), flip_t(Trans), N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   syr2k_entry<float>("exo_ssyr2k", Order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_dsyr2k(const enum CBLAS_ORDER Order, const enum CBLAS_UPLO Uplo, const enum CBLAS_TRANSPOSE Trans,
                 const int N, const int K, const double alpha, const double *A, const int lda, const double *B,
                 const int ldb, const double beta, double *C, const int ldc) {
+  if (col_major(Order)) return syr2k_entry<double>("exo_dsyr2k", kRowMajor, flip_u(Uplo), flip_t(Trans), N, K, alpha, A, lda, B, ldb, beta, C, ldc);
   syr2k_entry<double>("exo_dsyr2k", Order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 void exo_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE Side, const enum CBLAS_UPLO Uplo,
                const enum CBLAS_TRANSPOSE TransA, const enum CBLAS_DIAG Diag, const int M, const int N,
                const float alpha, const float *A, const int lda, float *B, const int ldb) {
+  if (col_major(Order)) return trmm_entry<float>("exo_strmm", kRowMajor, flip_s(Side), flip_u(Uplo), TransA, Diag, N, M, alpha, A, lda, B, ldb, true);
   trmm_entry<float>("exo_strmm", Order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb);
 }
 

@@ -247,26 +247,31 @@ void syr2k_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, lon
   launch<T>(n, n, 2 * k, alpha, ab, Transposed<T, Cat<T>>{ba}, beta, C, ldc, upper ? 2 : 1);
 }
 
-// src/level3/trmm.py:12-78 (Left): B = alpha op(A) B with A triangular.  B
+// src/level3/trmm.py:12-78 (Left): B = alpha op(A) B with A triangular
+// (right: B = alpha B op(A), used for column-major calls).  B
 // is copied to scratch first (the product reads every row of B while it is
 // overwritten).  Entries outside the triangle enter the product as zeros, so
 // an infinity or NaN in B reaches rows whose triangle excludes it; the
 // reference skips those terms.
 template <typename T>
-void trmm_simt(bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B, long ldb) {
+void trmm_simt(bool left, bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B,
+               long ldb) {
   if (m <= 0 || n <= 0) return;
   T *Bc = static_cast<T *>(scratch(sizeof(T) * size_t(m) * size_t(n)));
   EXB_CUDA(cudaMemcpy2DAsync(Bc, sizeof(T) * size_t(n), B, sizeof(T) * size_t(ldb), sizeof(T) * size_t(n), size_t(m),
                              cudaMemcpyDeviceToDevice, ctx().stream));
-  launch<T>(m, n, m, alpha, Tri<T>{A, lda, upper, trans, unit}, Plain<T>{Bc, n, false}, T(0), B, ldb, 4);
+  if (left)
+    launch<T>(m, n, m, alpha, Tri<T>{A, lda, upper, trans, unit}, Plain<T>{Bc, n, false}, T(0), B, ldb, 4);
+  else  // B = alpha B op(A), A n x n
+    launch<T>(m, n, n, alpha, Plain<T>{Bc, n, false}, Tri<T>{A, lda, upper, trans, unit}, T(0), B, ldb, 4);
 }
 
 template void syr2k_simt<float>(bool, bool, long, long, float, const float *, long, const float *, long, float,
                                 float *, long);
 template void syr2k_simt<double>(bool, bool, long, long, double, const double *, long, const double *, long, double,
                                  double *, long);
-template void trmm_simt<float>(bool, bool, bool, long, long, float, const float *, long, float *, long);
-template void trmm_simt<double>(bool, bool, bool, long, long, double, const double *, long, double *, long);
+template void trmm_simt<float>(bool, bool, bool, bool, long, long, float, const float *, long, float *, long);
+template void trmm_simt<double>(bool, bool, bool, bool, long, long, double, const double *, long, double *, long);
 template void gemm_simt<float>(bool, bool, long, long, long, float, const float *, long, const float *, long, float,
                                float *, long);
 template void gemm_simt<double>(bool, bool, long, long, long, double, const double *, long, const double *, long,

@@ -80,7 +80,8 @@ template <typename T>
 void syr2k_simt(bool upper, bool trans, long n, long k, T alpha, const T *A, long lda, const T *B, long ldb, T beta,
                 T *C, long ldc);
 template <typename T>
-void trmm_simt(bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B, long ldb);
+void trmm_simt(bool left, bool upper, bool trans, bool unit, long m, long n, T alpha, const T *A, long lda, T *B,
+               long ldb);
 // tcgen05 tensor-core paths: FP32 through three BF16 terms per operand
 void gemm_split_bf16(bool ta, bool tb, long m, long n, long k, float alpha, const float *A, long lda, const float *B,
                      long ldb, float beta, float *C, long ldc);

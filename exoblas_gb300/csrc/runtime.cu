@@ -84,6 +84,12 @@ static int initial_precision() {
   return EXOBLAS_PRECISION_NATIVE;
 }
 
+static int initial_column_major() {
+  const char *e = getenv("EXOBLAS_COLUMN_MAJOR");
+  return e && (!strcmp(e, "1") || !strcmp(e, "on")) ? 1 : 0;
+}
+static thread_local int tl_column_major = initial_column_major();
+
 constexpr int kMaxDevices = 64;
 static thread_local Context *tl_ctx[kMaxDevices] = {};
 struct CtxOwner {
@@ -95,6 +101,8 @@ struct CtxOwner {
   }
 };
 static thread_local CtxOwner tl_owner;
+
+bool column_major_enabled() { return tl_column_major != 0; }
 
 Context &ctx() {
   int dev = 0;
@@ -297,6 +305,13 @@ int exoblas_set_precision(int mode) {
     ctx().precision = mode;
   });
 }
+
+int exoblas_set_column_major(int enable) {
+  tl_column_major = enable ? 1 : 0;
+  return EXOBLAS_SUCCESS;
+}
+
+int exoblas_get_column_major(void) { return tl_column_major; }
 
 int exoblas_get_precision(void) {
   int p = EXOBLAS_PRECISION_NATIVE;

@@ -10,6 +10,8 @@
 namespace exb {
 
 void count_launch(unsigned n = 1);
+// column-major calls accepted on this thread (exoblas_set_column_major)
+bool column_major_enabled();
 // CTAs of `kernel` (threads per CTA, dynamic shared memory) resident at once
 // on one SM of the current device; cached per device and kernel.
 int resident_per_sm(const void *kernel, int threads, size_t smem = 0);

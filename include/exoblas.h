@@ -100,6 +100,14 @@ enum EXOBLAS_PRECISION { EXOBLAS_PRECISION_NATIVE = 0, EXOBLAS_PRECISION_SPLIT_B
 EXOBLAS_API int exoblas_set_precision(int mode);
 EXOBLAS_API int exoblas_get_precision(void);
 
+/* Column-major calls (CblasColMajor) for this thread: rejected by default,
+ * as the reference rejects them; when enabled every exo_* entry point with
+ * an Order argument computes the column-major (CBLAS) result by running the
+ * row-major call on the transposed view of its operands.  The environment
+ * variable EXOBLAS_COLUMN_MAJOR=1 enables it for every thread. */
+EXOBLAS_API int exoblas_set_column_major(int enable);
+EXOBLAS_API int exoblas_get_column_major(void);
+
 /* Number of CUDA kernels this library has launched in the calling process. */
 EXOBLAS_API unsigned long long exoblas_kernel_launches(void);
 /* Bytes this process has copied host->device and device->host while staging
