@@ -75,8 +75,15 @@ struct Params {
 // below (lower) or above (upper) the diagonal, two 64-wide n-tiles each.
 __device__ __forceinline__ void tile_mn(const Params &p, int t, int &mt, int &nt) {
   if (!p.tri) {
-    mt = t % p.mtiles;
-    nt = t / p.mtiles;
+    // groups of 8 m-tiles walked along n: the CTAs of one wave share a few
+    // A slabs and B slabs, so the digit planes are re-read from L2
+    constexpr int G = 8;
+    const int group = t / (G * p.ntiles);
+    const int first = group * G;
+    const int gm = p.mtiles - first < G ? p.mtiles - first : G;
+    const int in = t - group * G * p.ntiles;
+    mt = first + in % gm;
+    nt = in / gm;
     return;
   }
   const int b = t >> 1;

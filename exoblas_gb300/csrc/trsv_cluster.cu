@@ -1,21 +1,24 @@
 // Triangular solve (src/level2/trsv.py:10-52) for large n: blocked
-// substitution in one persistent launch of 8-CTA thread-block clusters.
+// substitution in one persistent launch of 16-CTA thread-block clusters
+// (8-CTA where fewer than four 16-CTA clusters fit).
 //
 // Effective-lower formulation as in trsv.cu: L(i, j) = trans ? A[c(j)][c(i)]
 // : A[c(i)][c(j)], c(k) = rev ? n-1-k : k, z = x in effective order.  Blocks
 // of kTB = 64 rows.  Roles, decided at run time so that the solver is always
 // a cluster that is already running:
 //
-//  * the first cluster to start is the SOLVER.  CTA r of it owns rows
-//    [8r, 8r+8) of every block.  Step K: rhs = b_K - (bulk partial sums of
-//    block row K) - L[K,K-2] x_{K-2} - L[K,K-1] x_{K-1}, exchanged between
-//    the 8 CTAs through distributed shared memory, then x_K = inv(L_KK) rhs
+//  * the first cluster to start is the SOLVER.  Each of its C CTAs owns
+//    64/C rows of every block.  Step K: rhs = b_K - (bulk partial sums of
+//    block row K) - L[K,K-kD..K-1] x, exchanged between the C CTAs through
+//    distributed shared memory, then x_K = inv(L_KK) rhs
 //    (the diagonal block solved in shared memory with its inverse, computed
 //    beforehand by trsv_inverse_kernel in the working precision), exchanged
-//    again and published to global memory with a release flag.  Everything
-//    except the L[K,K-1] product and the two exchanges is done in the
-//    shadow of the previous step's cluster barrier, and the operand rows the
-//    solver needs are prefetched kPre steps ahead with cp.async.
+//    again and published to global memory with a release flag.  With
+//    8-CTA clusters (solve_chain) everything except the L[K,K-1] product
+//    and the two exchanges runs in the shadow of the previous step's cluster
+//    barrier; with 16-CTA clusters (solve_chain2) dedicated critical and
+//    helper warps exchange through st.async stores counted on mbarriers.
+//    The operand rows the solver needs are prefetched with cp.async.
 //  * every other CTA STREAMS the bulk: work items (K, c) cover tiles
 //    L[K, J] for J in chunk c (kCT tiles) with J < K - kD, claimed in order of
 //    K (the step that needs them) through an atomic ticket.  An item writes
