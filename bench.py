@@ -69,15 +69,18 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=["bandwidth", "precision", "batch", "serve"], default="bandwidth",
+    ap.add_argument("--workload", choices=["bandwidth", "precision", "batch", "serve", "routines"],
+                    default="bandwidth",
                     help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set; batch: "
-                         "4096 mixed instances in one persistent launch; serve: a Poisson request stream")
+                         "4096 mixed instances in one persistent launch; serve: a Poisson request stream; "
+                         "routines: every other level-1/2 routine at HBM-sized operands")
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=20000.0, help="serve: mean arrivals per second")
     ap.add_argument("--workers", type=int, default=8, help="serve: server worker streams")
     ap.add_argument("--per-call-sample", type=int, default=2000, help="serve: requests timed per call")
     ap.add_argument("--size", type=int, default=8192, help="M = N = K of the precision set")
-    ap.add_argument("--kernels", default="", help="bandwidth: comma list, a subset of the set (profiling runs)")
+    ap.add_argument("--kernels", default="",
+                    help="bandwidth / routines: comma list, a subset of the set (profiling runs)")
     return ap.parse_args()
 
 
@@ -307,6 +310,8 @@ def main():
         return run_precision(args)
     if args.workload == "serve":
         return run_serve(args)
+    if args.workload == "routines":
+        return run_routines(args)
     if args.workload == "batch":
         return run_batch(args)
 
@@ -580,6 +585,142 @@ def run_precision(args):
         "results": out,
     }
     print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------- routines workload --
+def run_routines(args):
+    """Every level-1 / level-2 routine outside the bandwidth set, each on its
+    own device-resident operands larger than L2, timed alone with CUDA events
+    on the library's stream (mean over args.steps calls after args.warmup):
+    algorithmic bytes (each operand element read or written once) per call
+    over the call's time, against the measured HBM copy bandwidth.  Level 1
+    at n = 2^26 (f32) / 2^25 (f64); dense level 2 at 16384^2 (f32) /
+    11585^2 (f64, same bytes); banded level 2 at 2^21 rows, 32 off-diagonals
+    on each side (gbmv) or one side (sbmv, tbmv)."""
+    import torch
+
+    import exoblas_gb300 as eb
+    from exoblas_gb300 import _native
+
+    L = _native.lib()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    eb.set_stream(stream)
+    eb.set_blocking(False)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    vp = C.c_void_p
+
+    def u(nel, dt):
+        return torch.rand(int(nel), generator=g, device="cuda", dtype=dt).mul_(2).sub_(1)
+
+    res = torch.zeros(8, dtype=torch.float64, device="cuda")
+    r = vp(res.data_ptr())
+    f32, f64 = torch.float32, torch.float64
+    items = []  # (name, bytes, closure)
+
+    def level1(p, dt, n, es):
+        x, y = u(n, dt), u(n, dt)
+        P = torch.tensor([-1.0, 0.9, 0.1, -0.1, 0.9], dtype=dt, device="cuda")
+        X, Y, PP = vp(x.data_ptr()), vp(y.data_ptr()), vp(P.data_ptr())
+        items.extend([
+            (f"{p}asum", es * n, lambda: getattr(L, f"exoblas_{p}asum_device")(n, X, 1, r)),
+            (f"{p}copy", 2 * es * n, lambda: getattr(L, f"exo_{p}copy")(n, X, 1, Y, 1)),
+            (f"{p}swap", 4 * es * n, lambda: getattr(L, f"exo_{p}swap")(n, X, 1, Y, 1)),
+            (f"{p}scal", 2 * es * n, lambda: getattr(L, f"exo_{p}scal")(n, 0.5, X, 1)),
+            (f"{p}rot", 4 * es * n, lambda: getattr(L, f"exo_{p}rot")(n, X, 1, Y, 1, 0.8, 0.6)),
+            (f"{p}rotm", 4 * es * n, lambda: getattr(L, f"exo_{p}rotm")(n, X, 1, Y, 1, PP)),
+        ])
+        return x, y, P
+
+    def level2(p, dt, n, es):
+        A = u(n * n, dt)
+        x, y = u(n, dt), u(n, dt)
+        a, X, Y = vp(A.data_ptr()), vp(x.data_ptr()), vp(y.data_ptr())
+        tri = n * (n + 1) // 2
+        items.extend([
+            (f"{p}ger", es * (2 * n * n + 2 * n), lambda: getattr(L, f"exo_{p}ger")(101, n, n, 1e-3, X, 1, Y, 1, a, n)),
+            (f"{p}symv", es * (tri + 3 * n),
+             lambda: getattr(L, f"exo_{p}symv")(101, 121, n, 1.0, a, n, X, 1, 0.5, Y, 1)),
+            (f"{p}syr", es * (2 * tri + n), lambda: getattr(L, f"exo_{p}syr")(101, 122, n, 1e-3, X, 1, a, n)),
+            (f"{p}syr2", es * (2 * tri + 2 * n),
+             lambda: getattr(L, f"exo_{p}syr2")(101, 121, n, 1e-3, X, 1, Y, 1, a, n)),
+            (f"{p}trmv", es * (tri + 2 * n), lambda: getattr(L, f"exo_{p}trmv")(101, 121, 111, 131, n, a, n, X, 1)),
+        ])
+        return A, x, y
+
+    def banded(p, dt, n, k, es):
+        G = u(n * (2 * k + 1), dt)
+        B = u(n * (k + 1), dt)
+        x, y = u(n, dt), u(n, dt)
+        gp, bp, X, Y = vp(G.data_ptr()), vp(B.data_ptr()), vp(x.data_ptr()), vp(y.data_ptr())
+        items.extend([
+            (f"{p}gbmv", es * (n * (2 * k + 1) + 3 * n),
+             lambda: getattr(L, f"exo_{p}gbmv")(n, n, k, k, 1.0, gp, 2 * k + 1, X, 1, 0.5, Y, 1)),
+            (f"{p}sbmv", es * (n * (k + 1) + 3 * n),
+             lambda: getattr(L, f"exo_{p}sbmv")(101, 121, n, k, 1.0, bp, k + 1, X, 1, 0.5, Y, 1)),
+            (f"{p}tbmv", es * (n * (k + 1) + 2 * n),
+             lambda: getattr(L, f"exo_{p}tbmv")(101, 121, 111, 131, n, k, bp, k + 1, X, 1)),
+        ])
+        return G, B, x, y
+
+    want = set(args.kernels.split(",")) if args.kernels else None
+
+    def wanted(*names):
+        return want is None or any(nm in want for nm in names)
+
+    keep = []
+    for p, dt, es in (("s", f32, 4), ("d", f64, 8)):
+        if wanted(*(p + r for r in ("asum", "copy", "swap", "scal", "rot", "rotm"))):
+            keep.append(level1(p, dt, (1 << 26) if p == "s" else (1 << 25), es))
+        if wanted(*(p + r for r in ("ger", "symv", "syr", "syr2", "trmv"))):
+            keep.append(level2(p, dt, 16384 if p == "s" else 11585, es))
+        if wanted(*(p + r for r in ("gbmv", "sbmv", "tbmv"))):
+            keep.append(banded(p, dt, 1 << 21, 32, es))
+    if wanted("snrm2", "isamax", "dnrm2", "idamax"):
+        nrm = u(1 << 26, f32), u(1 << 25, f64)
+        keep.append(nrm)
+        items.append(("snrm2", 4 * (1 << 26), lambda: L.exo_snrm2(1 << 26, vp(nrm[0].data_ptr()), 1)))
+        items.append(("isamax", 4 * (1 << 26), lambda: L.exo_isamax(1 << 26, vp(nrm[0].data_ptr()), 1)))
+        items.append(("dnrm2", 8 * (1 << 25), lambda: L.exo_dnrm2(1 << 25, vp(nrm[1].data_ptr()), 1)))
+        items.append(("idamax", 8 * (1 << 25), lambda: L.exo_idamax(1 << 25, vp(nrm[1].data_ptr()), 1)))
+    if want is not None:
+        items[:] = [it for it in items if it[0] in want]
+    torch.cuda.synchronize()
+    hbm, peak_kind = peaks()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    K = max(3, min(args.steps, 50))
+    clocks = Clocks(0)
+    clocks.start()
+    time.sleep(0.25)
+    for name, nbytes, fn in items:
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        L.exoblas_synchronize()
+        e0.record(stream)
+        for _ in range(K):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if L.exoblas_get_status() != 0:
+            raise RuntimeError(f"library status {L.exoblas_get_status()} in {name}")
+        ms = e0.elapsed_time(e1) / K
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": round(ms, 4), "GB/s": round(gbs, 1), "frac_of_measured_hbm": round(gbs / hbm, 3)}
+    clk = clocks.stop()
+    tot_b = sum(b for _, b, _ in items)
+    tot_ms = sum(v["ms"] for v in out.values())
+    line = {
+        "metric": METRIC, "unit": UNIT, "value": round(tot_b / (tot_ms * 1e-3) / 1e9, 1), "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic (seeded uniform[-1,1))",
+        "config": {"workload": "routines: level-1 (2^26 f32 / 2^25 f64), dense level-2 (16384^2 f32 / 11585^2 f64), "
+                               "banded level-2 (2^21 rows, 32 off-diagonals), each call alone", "steps": K},
+        "peak": hbm, "peak_kind": peak_kind, "kernels": out, "clocks": clk,
+        "note": "nrm2 / i?amax results are read back by the entry point (a host synchronisation per call)",
+    }
+    print(json.dumps(line))
+    del keep
     return 0
 
 
