@@ -101,6 +101,10 @@ EXTRA = {
     "exoblas_sdot_device": ("i", "ipipip"),
     "exoblas_ddot_device": ("i", "ipipip"),
     "exoblas_dsdot_device": ("i", "ipipip"),
+    "exoblas_snrm2_device": ("i", "ipip"),
+    "exoblas_dnrm2_device": ("i", "ipip"),
+    "exoblas_isamax_device": ("i", "ipip"),
+    "exoblas_idamax_device": ("i", "ipip"),
     "exoblas_sgemv_noalloc": ("i", "iiiifpipifpip"),
     "exoblas_batch_plan_create": ("i", "pip"),
     "exoblas_batch_plan_run": ("i", "p"),

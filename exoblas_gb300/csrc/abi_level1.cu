@@ -77,6 +77,7 @@ static size_t iamax_entry(const char *fn, int N, const T *X, int incX) {
   return r;
 }
 
+
 // test/level1/axpy/exo_axpy_wrapper.h:5-34
 template <typename T>
 static void axpy_entry(const char *fn, int N, T alpha, const T *X, int incX, T *Y, int incY) {
@@ -240,6 +241,32 @@ static int asum_device(const char *fn, int N, const T *X, int incX, T *result) {
     l1::asum<T>(N, X, incX, result);
   });
 }
+// device-result forms (no host synchronisation), as exoblas_?asum_device
+template <typename T>
+static int nrm2_device(const char *fn, int N, const T *X, int incX, T *result) {
+  return guarded(fn, [&] {
+    require_device(result, "result must be a device pointer");
+    if (N < 1) {
+      EXB_CUDA(cudaMemsetAsync(result, 0, sizeof(T), ctx().stream));
+      return;
+    }
+    require_device(X, "X must be a device pointer");
+    X = rebase(X, N, incX);
+    l1::nrm2<T>(N, X, incX, result);
+  });
+}
+template <typename T>
+static int iamax_device(const char *fn, int N, const T *X, int incX, size_t *result) {
+  return guarded(fn, [&] {
+    require_device(result, "result must be a device pointer");
+    if (N < 1 || incX < 1) {
+      EXB_CUDA(cudaMemsetAsync(result, 0, sizeof(size_t), ctx().stream));
+      return;
+    }
+    require_device(X, "X must be a device pointer");
+    l1::iamax<T>(N, X, incX, result);
+  });
+}
 template <typename T>
 static int dot_device(const char *fn, int N, const T *X, int incX, const T *Y, int incY, T *result) {
   return guarded(fn, [&] {
@@ -324,6 +351,18 @@ void exo_drotm(const int N, double *X, const int incX, double *Y, const int incY
   rotm_entry<double>("exo_drotm", N, X, incX, Y, incY, P);
 }
 
+int exoblas_snrm2_device(const int N, const float *X, const int incX, float *result) {
+  return nrm2_device<float>("exoblas_snrm2_device", N, X, incX, result);
+}
+int exoblas_dnrm2_device(const int N, const double *X, const int incX, double *result) {
+  return nrm2_device<double>("exoblas_dnrm2_device", N, X, incX, result);
+}
+int exoblas_isamax_device(const int N, const float *X, const int incX, size_t *result) {
+  return iamax_device<float>("exoblas_isamax_device", N, X, incX, result);
+}
+int exoblas_idamax_device(const int N, const double *X, const int incX, size_t *result) {
+  return iamax_device<double>("exoblas_idamax_device", N, X, incX, result);
+}
 int exoblas_sasum_device(const int N, const float *X, const int incX, float *result) {
   return asum_device<float>("exoblas_sasum_device", N, X, incX, result);
 }

@@ -6,12 +6,13 @@
 //   lower (k)         A(r, c) at a[r * lda + k - (r - c)],    0 <= r - c <= k
 // Reference algorithms: src/level2/{gbmv,sbmv,tbmv,tbsv}.py.
 //
-// band_mv_kernel: a group of G lanes per output row walks the row's band
-// offsets d = c - i, accumulates in lane order and reduces with a fixed
-// shuffle tree (deterministic).  The general and the triangular NoTrans
-// bands are contiguous in a row of `a`; the symmetric and transposed ones
-// read the mirrored entries down a diagonal of the storage.  HBM-bound: the
-// band is read once (twice for sbmv's mirrored half, mostly from L2).
+// band_tile_kernel (narrow bands): a CTA stages the storage rows of 64 or
+// 128 output rows (plus the k mirrored rows before or after for sbmv and
+// transposed tbmv) in shared memory with coalesced reads and one thread per
+// output row walks its band offsets d = c - i in order.  band_mv_kernel
+// (wide bands): a group of G lanes per output row walks the offsets,
+// accumulates in lane order and reduces with a fixed shuffle tree.  Both
+// are deterministic and read the band from HBM about once.
 // tbsv_kernel: one warp per system, rows in dependency order, the band dot
 // of each row split over the lanes, the division by the pivot as in the
 // reference.
@@ -90,6 +91,128 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+__device__ __forceinline__ void cp_async_16(void *smem, const void *gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// Narrow bands: a CTA stages the storage rows its kTR output rows touch
+// (the rows themselves plus, for mirrored or transposed operators, the k
+// rows before or after) into shared memory with coalesced row reads, then
+// one thread per output row walks its band offsets from shared memory.
+template <typename T>
+struct Tile {
+  static constexpr int kTR = sizeof(T) == 4 ? 128 : 64;  // output rows (and threads) per CTA
+};
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(Tile<T>::kTR)
+    band_tile_kernel(long rows, long cols, long kl, long ku, T alpha, const T *__restrict__ a, long lda,
+                     const T *__restrict__ x, T beta, T *y, long incy, int flags, int W, int lo, int hi) {
+  constexpr int kTR = Tile<T>::kTR;
+  extern __shared__ __align__(16) unsigned char band_smem[];
+  T *tile = reinterpret_cast<T *>(band_smem);  // (kTR + lo + hi) storage rows x W
+  const int k = int(kl), xw_len = kTR + int(kl) + int(ku);
+  T *xw = tile + size_t(kTR + lo + hi) * W + 16 / sizeof(T);  // x[r0 - kl .. r0 + kTR + ku)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long dlo0, dhi0;
+  row_band<MODE>(kl, ku, flags, dlo0, dhi0);
+  const int nr = kTR + lo + hi;
+  const long ntiles = ceil_div(rows, long(kTR));
+  for (long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long r0 = t * kTR, q0 = r0 - lo;
+    // storage element e of the tile lands at tb[e - q0 * lda]; tb is shifted
+    // so that 16-byte aligned storage chunks land 16-byte aligned
+    constexpr int kPer = 16 / int(sizeof(T));
+    const int sh = lda == W ? int(((q0 * lda) % kPer + kPer) % kPer) : 0;
+    T *tb = tile + sh;
+    __syncthreads();  // the previous tile's reads are done
+    // asynchronous copies, all in flight at once
+    if (lda == W) {
+      // the tile is one contiguous span of the storage: 16-byte copies for
+      // its aligned body, element copies for the ends and zeros outside
+      const long s0 = q0 * lda, s1 = s0 + long(nr) * W;  // storage elements [s0, s1)
+      const long lo_in = s0 > 0 ? s0 : 0, hi_in = s1 < rows * lda ? s1 : rows * lda;
+      long b0 = (lo_in + kPer - 1) / kPer * kPer, b1 = hi_in / kPer * kPer;
+      const bool a16 = (reinterpret_cast<uintptr_t>(a) & 15u) == 0;
+      if (!a16 || b1 < b0) b0 = b1 = lo_in;  // no aligned body: element copies only
+      for (long e = s0 + threadIdx.x; e < s1; e += kTR) {
+        if (e < lo_in || e >= hi_in)
+          tb[e - s0] = T(0);
+        else if (e < b0 || e >= b1)
+          cp_async_elem(&tb[e - s0], a + e);
+      }
+      for (long c = b0 + long(threadIdx.x) * kPer; c < b1; c += long(kTR) * kPer)
+        cp_async_16(&tb[c - s0], a + c);
+    } else {
+      for (int rr = warp; rr < nr; rr += kTR / 32) {
+        const long q = q0 + rr;
+        const bool in = q >= 0 && q < rows;
+        for (int j = lane; j < W; j += 32) {
+          if (in)
+            cp_async_elem(&tb[rr * W + j], a + q * lda + j);
+          else
+            tb[rr * W + j] = T(0);
+        }
+      }
+    }
+    for (int e = threadIdx.x; e < xw_len; e += kTR) {
+      const long c = r0 - kl + e;
+      if (c >= 0 && c < cols)
+        cp_async_elem(&xw[e], x + c);
+      else
+        xw[e] = T(0);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    const long i = r0 + threadIdx.x;
+    if (i < rows) {
+      const int dlo = int(dlo0 > -i ? dlo0 : -i);
+      const int dhi = int(dhi0 < cols - 1 - i ? dhi0 : cols - 1 - i);
+      // Along d the shared-memory address is affine on each side of the
+      // diagonal: step 1 where the entry sits in row i's own storage row,
+      // step W - 1 where it is mirrored from row i + d.  Two segments at most.
+      const int ti = int(i - r0) + lo;  // row i's storage row within the tile
+      const T *xi = xw + (int(i - r0) + k);  // xi[d] = x[i + d]
+      const bool unit = MODE == kTriangular && (flags & kUnitBit);
+      T acc = T(0);
+      auto run = [&](int da, int db, int addr, int step) {
+#pragma unroll 4
+        for (int d = da; d <= db; ++d) {
+          const T v = (unit && d == 0) ? T(1) : tb[addr + (d - da) * step];
+          acc = fma(v, xi[d], acc);
+        }
+      };
+      const bool upper = flags & kUpperBit;
+      if (MODE == kGeneral) {
+        run(dlo, dhi, ti * W + dlo + k, 1);
+      } else if (MODE == kSymmetric) {
+        if (upper) {  // d < 0 mirrored (j = -d), d >= 0 direct (j = d)
+          run(dlo, dhi < -1 ? dhi : -1, ti * W + dlo * (W - 1), W - 1);
+          run(dlo > 0 ? dlo : 0, dhi, ti * W + (dlo > 0 ? dlo : 0), 1);
+        } else {  // d <= 0 direct (j = k + d), d > 0 mirrored (j = k - d)
+          run(dlo, dhi < 0 ? dhi : 0, ti * W + k + dlo, 1);
+          run(dlo > 1 ? dlo : 1, dhi, ti * W + k + (dlo > 1 ? dlo : 1) * (W - 1), W - 1);
+        }
+      } else if (!(flags & kTransBit)) {  // direct: j = d (upper), k + d (lower)
+        run(dlo, dhi, ti * W + (upper ? 0 : k) + dlo, 1);
+      } else {  // mirrored from row i + d: j = -d (upper), k - d (lower)
+        run(dlo, dhi, ti * W + (upper ? 0 : k) + dlo * (W - 1), W - 1);
+      }
+      T *yi = y + i * incy;
+      *yi = MODE == kTriangular ? acc : beta * *yi + alpha * acc;
+    }
+  }
+}
+
 // op(A) x = b in place, one warp: forward when the operator is lower
 // triangular (Lower/NoTrans, Upper/Trans), backward otherwise.  xs holds
 // the solution as it forms (unit stride); x (stride incx) receives it too.
@@ -134,6 +257,23 @@ static void launch(long rows, long cols, long kl, long ku, T alpha, const T *a, 
                    long incy, int flags) {
   if (rows <= 0) return;
   const long width = MODE == kGeneral ? kl + ku + 1 : (MODE == kSymmetric ? 2 * kl + 1 : kl + 1);
+  // narrow bands: shared-memory tiles (at most 48 KB per CTA)
+  const long W = MODE == kGeneral ? kl + ku + 1 : kl + 1;  // storage row width
+  const bool mirrored = MODE == kSymmetric || (MODE == kTriangular && (flags & kTransBit));
+  const bool before = mirrored && (MODE == kSymmetric ? bool(flags & kUpperBit) : bool(flags & kUpperBit));
+  const long lo = mirrored && before ? kl : 0, hi = mirrored && !before ? kl : 0;
+  constexpr int kTR = Tile<T>::kTR;
+  const size_t smem = (size_t(kTR + lo + hi) * size_t(W) + size_t(kTR + kl + ku)) * sizeof(T) + 16;
+  if (smem <= 48 * 1024) {
+    const long ntiles = ceil_div(rows, long(kTR));
+    const int per_sm = resident_per_sm(reinterpret_cast<const void *>(band_tile_kernel<T, MODE>), kTR, smem);
+    long blocks = ntiles < long(ctx().sm_count) * per_sm ? ntiles : long(ctx().sm_count) * per_sm;
+    band_tile_kernel<T, MODE><<<int(blocks), kTR, smem, ctx().stream>>>(rows, cols, kl, ku, alpha, a, lda, x, beta, y,
+                                                                       incy, flags, int(W), int(lo), int(hi));
+    EXB_LAUNCH("band tile kernel");
+    count_launch();
+    return;
+  }
   const int G = width >= 48 ? 32 : 4;
   const long rpb = (kThreads / 32) * (32 / G);
   long blocks = ceil_div(rows, rpb);

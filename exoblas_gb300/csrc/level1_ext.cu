@@ -5,14 +5,19 @@
 // element of largest magnitude, NaNs never win except a NaN in the first
 // position (the sequential loop starts from |x[0]| and tests `>`).
 //
-// Both are one streaming pass with per-thread partials, a fixed-order warp
-// and block combination and a last-arriving-CTA combination of the per-CTA
-// partials in CTA order (deterministic).  nrm2 accumulates the squares in
-// FP64: exact enough and overflow-free for FP32 inputs; for FP64 inputs
-// whose largest magnitude lies outside [2^-490, 2^490] (the squares could
-// overflow or underflow) a second pass rescales by a power of two, launched
-// always and returning at once unless the first pass asked for it, so the
-// call never waits on the host.
+// Both are one streaming pass (16-byte vector loads for unit stride) with
+// per-thread partials, a fixed-order warp and block combination and a
+// last-arriving-CTA combination of the per-CTA partials in CTA order
+// (deterministic).  Per element they do little floating-point work -- this
+// GPU's FP64 pipe is far slower than HBM: magnitudes are compared as
+// integer bit patterns, and FP32 squares are accumulated exactly as FP32
+// pairs (product error through fma, TwoSum), FP64 squares with one FMA.
+// When the largest magnitude lies outside [2^-40, 2^40] (FP32) or
+// [2^-490, 2^490] (FP64), where sums of squares could overflow or lose the
+// small terms to underflow, a
+// second pass rescales by a power of two; it is launched always and returns
+// at once unless the first pass asked for it, so the call never waits on
+// the host.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -27,8 +32,54 @@ namespace l1 {
 namespace ext {
 
 constexpr int kT = 256;
+constexpr int kU = 4;  // vectors in flight per thread
 
 __device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
+
+// magnitude keys: |x| as an unsigned bit pattern orders like |x| for every
+// non-NaN value, and every NaN's key is above the infinity's
+template <typename T>
+struct Key;
+template <>
+struct Key<float> {
+  using U = unsigned;
+  static constexpr U kInf = 0x7f800000u;
+  static __device__ __forceinline__ U of(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+  static __device__ __forceinline__ double value(U k) { return double(__uint_as_float(k)); }
+};
+template <>
+struct Key<double> {
+  using U = unsigned long long;
+  static constexpr U kInf = 0x7ff0000000000000ull;
+  static __device__ __forceinline__ U of(double x) { return U(__double_as_longlong(x)) & 0x7fffffffffffffffull; }
+  static __device__ __forceinline__ double value(U k) { return __longlong_as_double((long long)k); }
+};
+
+// sum of squares: FP32 inputs through exact products p + e (e = fma(x, x, -p))
+// accumulated with TwoSum in an FP32 pair (no FP64 work per element); FP64
+// inputs with one FP64 FMA per element.  The largest magnitude is kept as
+// an integer key (no floating-point work).
+template <typename T>
+struct SumSq;
+template <>
+struct SumSq<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float p = x * x;
+    const float e = fmaf(x, x, -p);
+    const float s = hi + p;
+    const float z = s - hi;
+    lo += ((hi - (s - z)) + (p - z)) + e;
+    hi = s;
+  }
+  __device__ __forceinline__ double get() const { return double(hi) + double(lo); }
+};
+template <>
+struct SumSq<double> {
+  double ss = 0.0;
+  __device__ __forceinline__ void add(double x) { ss = fma(x, x, ss); }
+  __device__ __forceinline__ double get() const { return ss; }
+};
 
 struct Part2 {
   double ss, mx;
@@ -53,38 +104,97 @@ __device__ __forceinline__ Part2 part2_reduce_block(Part2 v, Part2 *sh) {
   return r;  // valid in thread 0
 }
 
+// Calls f(slot, value, index) for this thread's elements: 16-byte vectors
+// when x is unit-stride and aligned, kU of them consumed per step while the
+// next kU are in flight; slot u < kU names an independent accumulator (the
+// elements of one slot come in increasing index order).
+template <typename T, class F>
+__device__ __forceinline__ void for_each(long n, const T *__restrict__ x, long inc, bool vec, F &&f) {
+  using V = typename V16<T>::type;
+  constexpr int VN = V16<T>::N;
+  const long stride = long(gridDim.x) * kT;
+  const long gt = long(blockIdx.x) * kT + threadIdx.x;
+  if (vec) {
+    const long nvec = n / VN;
+    const V *xv = reinterpret_cast<const V *>(x);
+    long v = gt;
+    // the next kU vectors are loaded before the current ones are consumed
+    V a[kU], b[kU];
+    bool have = v + (kU - 1) * stride < nvec;
+    if (have) {
+#pragma unroll
+      for (int u = 0; u < kU; ++u) a[u] = ld_stream(xv + v + u * stride);
+    }
+    while (have) {
+      const long vn = v + kU * stride;
+      const bool more = vn + (kU - 1) * stride < nvec;
+      if (more) {
+#pragma unroll
+        for (int u = 0; u < kU; ++u) b[u] = ld_stream(xv + vn + u * stride);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+#pragma unroll
+        for (int e = 0; e < VN; ++e) f(u, vget<T>(a[u], e), (v + u * stride) * VN + e);
+#pragma unroll
+      for (int u = 0; u < kU; ++u) a[u] = b[u];
+      v = vn;
+      have = more;
+    }
+    for (; v < nvec; v += stride) {
+      const V c = ld_stream(xv + v);
+#pragma unroll
+      for (int e = 0; e < VN; ++e) f(0, vget<T>(c, e), v * VN + e);
+    }
+    for (long i = nvec * VN + gt; i < n; i += stride) f(0, x[i], i);
+  } else {
+    for (long i = gt; i < n; i += stride) f(0, x[i * inc], i);
+  }
+}
+
 // pass 1: sum of squares and largest magnitude.  flag[0] receives the
 // binary exponent to rescale by (0: not needed).
 template <typename T>
-__global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ x, long inc, Part2 *partials,
-                                                  unsigned *counter, T *result, int *flag) {
+__global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ x, long inc, bool vec,
+                                                  Part2 *partials, unsigned *counter, T *result, int *flag) {
+  using K = Key<T>;
   __shared__ Part2 sh[kT / 32];
   __shared__ bool last;
-  Part2 acc{0.0, 0.0};
-  for (long i = long(blockIdx.x) * kT + threadIdx.x; i < n; i += long(gridDim.x) * kT) {
-    const double v = fabs(double(x[i * inc]));
-    acc.ss = fma(v, v, acc.ss);
-    acc.mx = nan_max(acc.mx, v);
-  }
-  Part2 tot = part2_reduce_block(acc, sh);
+  SumSq<T> acc[kU];
+  typename K::U mk = 0;
+  for_each(n, x, inc, vec, [&](int u, T v, long) {
+    acc[u].add(v);
+    const typename K::U k = K::of(v);
+    mk = k > mk ? k : mk;
+  });
+  double ss = 0.0;
+#pragma unroll
+  for (int u = 0; u < kU; ++u) ss += acc[u].get();
+  Part2 tot = part2_reduce_block(Part2{ss, K::value(mk)}, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = tot;
     __threadfence();
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  Part2 g{0.0, 0.0};
-  for (unsigned b = 0; b < gridDim.x; ++b) {
-    const Part2 p = partials[b];
-    g.ss += p.ss;
-    g.mx = nan_max(g.mx, p.mx);
+  // the last CTA combines the per-CTA partials: thread t takes CTAs t,
+  // t + kT, ... in order, then the fixed block tree
+  Part2 mine{0.0, 0.0};
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) {
+    const Part2 p{__ldcg(&partials[b].ss), __ldcg(&partials[b].mx)};
+    mine.ss += p.ss;
+    mine.mx = nan_max(mine.mx, p.mx);
   }
+  const Part2 g = part2_reduce_block(mine, sh);
+  if (threadIdx.x != 0) return;
   *counter = 0;
+  // squares and per-thread sums of up to 2^20 of them stay in range and
+  // normal while the largest magnitude lies in [tiny, lim]
+  const double lim = sizeof(T) == 8 ? 0x1p490 : 0x1p40, tiny = sizeof(T) == 8 ? 0x1p-490 : 0x1p-40;
   int e = 0;
-  if (sizeof(T) == 8 && g.mx == g.mx && g.mx != INFINITY && g.mx != 0.0 &&
-      (g.mx > 0x1p490 || g.mx < 0x1p-490)) {
+  if (g.mx == g.mx && g.mx != INFINITY && g.mx != 0.0 && (g.mx > lim || g.mx < tiny)) {
     e = ilogb(g.mx);
     if (e == 0) e = 1;  // 0 means "no rescale"
   }
@@ -97,85 +207,113 @@ __global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ 
     *result = T(sqrt(g.ss));
 }
 
-// pass 2 (FP64 only, when pass 1 asked for it): sum of (x 2^-e)^2
+// pass 2 (when pass 1 asked for it): sum of (x 2^-e)^2
 template <typename T>
-__global__ void __launch_bounds__(kT) nrm2_rescaled_kernel(long n, const T *__restrict__ x, long inc, Part2 *partials,
-                                                           unsigned *counter, T *result, const int *flag) {
+__global__ void __launch_bounds__(kT) nrm2_rescaled_kernel(long n, const T *__restrict__ x, long inc, bool vec,
+                                                           Part2 *partials, unsigned *counter, T *result,
+                                                           const int *flag) {
   __shared__ Part2 sh[kT / 32];
   __shared__ bool last;
   const int e = *flag;
   if (e == 0) return;
-  Part2 acc{0.0, 0.0};
-  for (long i = long(blockIdx.x) * kT + threadIdx.x; i < n; i += long(gridDim.x) * kT) {
-    const double v = ldexp(fabs(double(x[i * inc])), -e);
-    acc.ss = fma(v, v, acc.ss);
-  }
-  Part2 tot = part2_reduce_block(acc, sh);
+  const T sc = T(ldexp(1.0, -e));  // exact power of two
+  SumSq<T> acc[kU];
+  for_each(n, x, inc, vec, [&](int u, T v, long) { acc[u].add(v * sc); });
+  double ss0 = 0.0;
+#pragma unroll
+  for (int u = 0; u < kU; ++u) ss0 += acc[u].get();
+  Part2 tot = part2_reduce_block(Part2{ss0, 0.0}, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = tot;
     __threadfence();
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  double ss = 0.0;
-  for (unsigned b = 0; b < gridDim.x; ++b) ss += partials[b].ss;
+  Part2 mine{0.0, 0.0};
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) mine.ss += __ldcg(&partials[b].ss);
+  const double ss = part2_reduce_block(mine, sh).ss;
+  if (threadIdx.x != 0) return;
   *counter = 0;
   *const_cast<int *>(flag) = 0;  // every CTA has read it; the word returns to zero
   *result = T(ldexp(sqrt(ss), e));
 }
 
-template <typename T>
+template <typename U>
 struct Best {
-  T v;
+  U k;  // magnitude key (0 before any element: no non-NaN key is below it... see better())
   long i;
 };
 
-template <typename T>
-__device__ __forceinline__ Best<T> better(Best<T> a, Best<T> b) {
-  return (b.v > a.v || (b.v == a.v && b.i < a.i)) ? b : a;
+// larger magnitude wins; equal magnitudes: the smaller index
+template <typename U>
+__device__ __forceinline__ Best<U> better(Best<U> a, Best<U> b) {
+  return (b.k > a.k || (b.k == a.k && b.i < a.i)) ? b : a;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kT) iamax_kernel(long n, const T *__restrict__ x, long inc, Best<T> *partials,
-                                                   unsigned *counter, size_t *result) {
-  __shared__ Best<T> sh[kT / 32];
+__global__ void __launch_bounds__(kT) iamax_kernel(long n, const T *__restrict__ x, long inc, bool vec,
+                                                   Best<typename Key<T>::U> *partials, unsigned *counter,
+                                                   size_t *result) {
+  using K = Key<T>;
+  using U = typename K::U;
+  __shared__ Best<U> sh[kT / 32];
   __shared__ bool last;
-  Best<T> acc{T(-1), LONG_MAX};
-  for (long i = long(blockIdx.x) * kT + threadIdx.x; i < n; i += long(gridDim.x) * kT) {
-    const T v = fabs(x[i * inc]);
-    if (v > acc.v) acc = Best<T>{v, i};  // increasing i: the first of equal values stays
-  }
+  // keys are stored + 1 so that 0 means "none yet"; NaN keys never enter
+  Best<U> accs[kU];
+#pragma unroll
+  for (int u = 0; u < kU; ++u) accs[u] = Best<U>{0, LONG_MAX};
+  for_each(n, x, inc, vec, [&](int u, T v, long i) {
+    const U k = K::of(v) + 1;
+    if (k <= K::kInf + 1 && k > accs[u].k) accs[u] = Best<U>{k, i};  // per slot increasing i: the first stays
+  });
+  Best<U> acc = accs[0];
+#pragma unroll
+  for (int u = 1; u < kU; ++u) acc = better(acc, accs[u]);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    Best<T> other{__shfl_xor_sync(0xffffffffu, acc.v, o), __shfl_xor_sync(0xffffffffu, acc.i, o)};
+    Best<U> other{__shfl_xor_sync(0xffffffffu, acc.k, o), __shfl_xor_sync(0xffffffffu, acc.i, o)};
     acc = better(acc, other);
   }
   if (lane == 0) sh[w] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    Best<T> b = sh[0];
-    for (int k = 1; k < kT / 32; ++k) b = better(b, sh[k]);
+    Best<U> b = sh[0];
+    for (int q = 1; q < kT / 32; ++q) b = better(b, sh[q]);
     partials[blockIdx.x] = b;
     __threadfence();
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || threadIdx.x != 0) return;
+  if (!last) return;
   __threadfence();
-  Best<T> g = partials[0];
-  for (unsigned b = 1; b < gridDim.x; ++b) g = better(g, partials[b]);
+  // the last CTA: thread t combines CTAs t, t + kT, ..., then warp and
+  // block trees (`better` is order-independent: larger key, then smaller index)
+  Best<U> g{0, LONG_MAX};
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT)
+    g = better(g, Best<U>{__ldcg(&partials[b].k), __ldcg(&partials[b].i)});
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    Best<U> other{__shfl_xor_sync(0xffffffffu, g.k, o), __shfl_xor_sync(0xffffffffu, g.i, o)};
+    g = better(g, other);
+  }
+  __syncthreads();  // sh is reused
+  if (lane == 0) sh[w] = g;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int q = 0; q < kT / 32; ++q) g = better(g, sh[q]);
   *counter = 0;
   const T x0 = x[0];
   *result = (x0 != x0 || g.i == LONG_MAX) ? size_t(0) : size_t(g.i);
 }
 
-inline long grid_for(long n) {
-  long blocks = ceil_div(n, long(kT) * 4);
+inline long grid_for(long n, const void *kernel) {
+  long blocks = ceil_div(n, long(kT) * 16);
   if (blocks < 1) blocks = 1;
-  if (blocks > grid_cap(4)) blocks = grid_cap(4);
+  const int per_sm = resident_per_sm(kernel, kT);
+  if (blocks > grid_cap(per_sm)) blocks = grid_cap(per_sm);
   return blocks;
 }
 
@@ -185,26 +323,26 @@ template <typename T>
 void nrm2(long n, const T *x, long incx, T *result) {
   using namespace ext;
   cudaStream_t s = ctx().stream;
-  const long blocks = grid_for(n);
+  const long blocks = grid_for(n, reinterpret_cast<const void *>(nrm2_kernel<T>));
+  const bool vec = incx == 1 && aligned16(x);
   Part2 *partials = static_cast<Part2 *>(scratch(sizeof(Part2) * size_t(blocks)));
   unsigned *counter = zero_words(2);
   int *flag = reinterpret_cast<int *>(counter + 1);
-  nrm2_kernel<T><<<int(blocks), kT, 0, s>>>(n, x, incx, partials, counter, result, flag);
-  count_launch();
-  if (sizeof(T) == 8) {
-    nrm2_rescaled_kernel<T><<<int(blocks), kT, 0, s>>>(n, x, incx, partials, counter, result, flag);
-    count_launch();
-  }
+  nrm2_kernel<T><<<int(blocks), kT, 0, s>>>(n, x, incx, vec, partials, counter, result, flag);
+  nrm2_rescaled_kernel<T><<<int(blocks), kT, 0, s>>>(n, x, incx, vec, partials, counter, result, flag);
   EXB_LAUNCH("nrm2 kernel");
+  count_launch(2);
 }
 
 template <typename T>
 void iamax(long n, const T *x, long incx, size_t *result) {
   using namespace ext;
-  const long blocks = grid_for(n);
-  Best<T> *partials = static_cast<Best<T> *>(scratch(sizeof(Best<T>) * size_t(blocks)));
+  using U = typename Key<T>::U;
+  const long blocks = grid_for(n, reinterpret_cast<const void *>(iamax_kernel<T>));
+  const bool vec = incx == 1 && aligned16(x);
+  Best<U> *partials = static_cast<Best<U> *>(scratch(sizeof(Best<U>) * size_t(blocks)));
   unsigned *counter = zero_words(1);
-  iamax_kernel<T><<<int(blocks), kT, 0, ctx().stream>>>(n, x, incx, partials, counter, result);
+  iamax_kernel<T><<<int(blocks), kT, 0, ctx().stream>>>(n, x, incx, vec, partials, counter, result);
   EXB_LAUNCH("iamax kernel");
   count_launch();
 }

@@ -161,6 +161,11 @@ EXOBLAS_API int exoblas_dasum_device(const int N, const double *X, const int inc
 EXOBLAS_API int exoblas_sdot_device(const int N, const float *X, const int incX, const float *Y, const int incY, float *result);
 EXOBLAS_API int exoblas_ddot_device(const int N, const double *X, const int incX, const double *Y, const int incY, double *result);
 EXOBLAS_API int exoblas_dsdot_device(const int N, const float *X, const int incX, const float *Y, const int incY, double *result);
+/* device-result nrm2 / i?amax (same semantics as exo_?nrm2 / exo_i?amax) */
+EXOBLAS_API int exoblas_snrm2_device(const int N, const float *X, const int incX, float *result);
+EXOBLAS_API int exoblas_dnrm2_device(const int N, const double *X, const int incX, double *result);
+EXOBLAS_API int exoblas_isamax_device(const int N, const float *X, const int incX, size_t *result);
+EXOBLAS_API int exoblas_idamax_device(const int N, const double *X, const int incX, size_t *result);
 
 /* ------------------------------------------------------------ level 2 --- */
 /* test/level2/gemv/exo_gemv_wrapper.h:7-39 */

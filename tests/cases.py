@@ -321,7 +321,7 @@ def nrm2_cases(p, Ns=(1, 2, 7, 100, 1000, 20000), incs=(1, 3, -1, 0), scales=(1.
     underflow, and non-positive increments (result 0)."""
     for n, inc, sc in itertools.product(Ns, incs, scales):
         if p == "s" and sc != 1.0:
-            continue
+            sc = 1e30 if sc > 1 else 1e-30  # FP32 magnitudes whose squares overflow / underflow
         g = rng(_seed("nrm2", p, n, inc, sc))
         x = (buf(g, n, max(abs(inc), 1), np.float64) * sc).astype(DT[p])
         yield Case(p + "nrm2", [n, x, inc], [], scalar=True, nred=n, label=f"n={n} inc={inc} scale={sc:g}")
