@@ -251,90 +251,140 @@ void syr2(bool upper, long n, T alpha, const T *x, long incx, const T *y, long i
 
 // ------------------------------------------------------------------- symv --
 // src/level2/symv.py:10-35.  The stored triangle is cut into 64 x 64 tiles;
-// each CTA reads one tile once and produces both its row contribution
-// (A_t x_cols) and, for off-diagonal tiles, its column contribution
-// (A_t^T x_rows).  Output row tile r receives one contribution per tile index
-// c (slot c): P[c][rows of r].  A second kernel sums the slots in order.
+// a CTA walks a strip of kSymStrip consecutive tiles of one storage tile
+// row, reading each tile once: the tile's row contribution (A_t x_cols)
+// accumulates across the strip in shared memory, its column contribution
+// (A_t^T x_rows, off-diagonal tiles) is written at once.  Output row tile r
+// receives one contribution per tile index c (slot c): P[c][rows of r]; a
+// strip's row sum goes to the slot of its first tile and its other slots
+// of that row tile are zero.  A second kernel sums the slots in order.
 constexpr int kSymTile = 64;
+constexpr int kSymStrip = 4;
+
+template <typename T, bool VEC, int PASSES, int VN, int RPP>
+__device__ __forceinline__ void symv_load(T (&av)[PASSES][VN], long n, long r0, long c0e, const T *__restrict__ A,
+                                          long lda) {
+  using V = typename V16<T>::type;
+#pragma unroll
+  for (int p = 0; p < PASSES; ++p) {
+    const long r = r0 + p * RPP;
+    if (r < n && VEC && c0e + VN <= n) {
+      const V v = ld_stream(reinterpret_cast<const V *>(A + r * lda + c0e));
+#pragma unroll
+      for (int e = 0; e < VN; ++e) av[p][e] = vget<T>(v, e);
+    } else {
+#pragma unroll
+      for (int e = 0; e < VN; ++e) av[p][e] = (r < n && c0e + e < n) ? A[r * lda + c0e + e] : T(0);
+    }
+  }
+}
+
+// One tile's products: row partials accumulate in rowacc (per pass, over
+// this thread's columns), column partials in colacc.  DIAG masks the half of
+// a diagonal tile outside the stored triangle (and its diagonal for the
+// column product, which the row product already holds).
+template <bool DIAG, typename T, int PASSES, int VN, int RPP>
+__device__ __forceinline__ void symv_tile(T (&av)[PASSES][VN], T (&xc)[VN], T (&xr)[PASSES],
+                                          T (&rowacc)[PASSES], T (&colacc)[VN], int cl, int rl, bool upper) {
+#pragma unroll
+  for (int p = 0; p < PASSES; ++p) {
+    const int r = rl + p * RPP;  // row within the tile
+#pragma unroll
+    for (int e = 0; e < VN; ++e) {
+      const int c = cl + e;  // column within the tile
+      const T a = av[p][e];
+      if (DIAG) {
+        const bool in_row = upper ? c >= r : c <= r;
+        const bool in_col = upper ? c > r : c < r;
+        rowacc[p] = fma(in_row ? a : T(0), xc[e], rowacc[p]);
+        colacc[e] = fma(in_col ? a : T(0), xr[p], colacc[e]);
+      } else {
+        rowacc[p] = fma(a, xc[e], rowacc[p]);
+        colacc[e] = fma(a, xr[p], colacc[e]);
+      }
+    }
+  }
+}
 
 template <typename T, bool VEC>
 __global__ void __launch_bounds__(kThreads)
-    symv_tile_kernel(long n, const T *__restrict__ A, long lda, const T *__restrict__ x, T *__restrict__ P, bool upper) {
+    symv_strip_kernel(long n, long nt, const T *__restrict__ A, long lda, const T *__restrict__ x, T *__restrict__ P,
+                      bool upper) {
   constexpr int VN = V16<T>::N;
   constexpr int TPR = kSymTile / VN;       // threads per tile row (16 float, 32 double)
   constexpr int RPP = kThreads / TPR;      // rows per pass
   constexpr int PASSES = kSymTile / RPP;
-  using V = typename V16<T>::type;
   __shared__ T colsh[RPP][kSymTile];
-  __shared__ T rowsh[kSymTile];
-  // tile index -> (bi, bj) of the lower triangle of tiles
-  const long k = blockIdx.x;
-  long bi = long((sqrt(8.0 * double(k) + 1.0) - 1.0) * 0.5);
-  while (bi * (bi + 1) / 2 > k) --bi;
-  while ((bi + 1) * (bi + 2) / 2 <= k) ++bi;
-  const long bj = k - bi * (bi + 1) / 2;
-  // stored tile: lower -> rows bi, cols bj; upper -> rows bj, cols bi
-  const long tr = upper ? bj : bi, tc = upper ? bi : bj;
-  const bool diag = bi == bj;
+  __shared__ T rowpart[kSymTile][TPR + 1];
+  __shared__ T diagcol[kSymTile];
+  const long strips = ceil_div(nt, long(kSymStrip));
+  const long tr = long(blockIdx.x) / strips, s = long(blockIdx.x) % strips;
+  // stored tiles of storage tile row tr: lower tc in [0, tr], upper [tr, nt)
+  const long t_lo = upper ? tr : 0, t_hi = upper ? nt - 1 : tr;
+  const long c0 = t_lo + s * kSymStrip;
+  if (c0 > t_hi) return;
+  const long c1 = c0 + kSymStrip - 1 < t_hi ? c0 + kSymStrip - 1 : t_hi;
   const int tx = threadIdx.x % TPR, ty = threadIdx.x / TPR;
-  const long c0 = tc * kSymTile + tx * VN;
-  T colacc[VN];
-#pragma unroll
-  for (int e = 0; e < VN; ++e) colacc[e] = 0;
-  T xc[VN];
-#pragma unroll
-  for (int e = 0; e < VN; ++e) xc[e] = c0 + e < n ? x[c0 + e] : T(0);
+  const long r0 = tr * kSymTile + ty;
+  T xr[PASSES], rowacc[PASSES];
 #pragma unroll
   for (int p = 0; p < PASSES; ++p) {
-    const int rr = p * RPP + ty;
-    const long r = tr * kSymTile + rr;
-    T av[VN];
-    if (r < n) {
-      const T *a = A + r * lda + c0;
-      if (VEC && c0 + VN <= n) {
-        V v = ld_stream(reinterpret_cast<const V *>(a));
-#pragma unroll
-        for (int e = 0; e < VN; ++e) av[e] = vget<T>(v, e);
-      } else {
-#pragma unroll
-        for (int e = 0; e < VN; ++e) av[e] = c0 + e < n ? a[e] : T(0);
-      }
-    } else {
-#pragma unroll
-      for (int e = 0; e < VN; ++e) av[e] = 0;
-    }
-    const T xr = r < n ? x[r] : T(0);
-    T rowacc = 0;
+    const long r = r0 + p * RPP;
+    xr[p] = r < n ? x[r] : T(0);
+    rowacc[p] = T(0);
+  }
+  if (threadIdx.x < kSymTile) diagcol[threadIdx.x] = T(0);
+  T av[PASSES][VN], an[PASSES][VN];
+  symv_load<T, VEC, PASSES, VN, RPP>(av, n, r0, c0 * kSymTile + tx * VN, A, lda);
+  for (long tc = c0; tc <= c1; ++tc) {
+    // next tile's rows in flight while this one is multiplied
+    if (tc < c1) symv_load<T, VEC, PASSES, VN, RPP>(an, n, r0, (tc + 1) * kSymTile + tx * VN, A, lda);
+    const long c0e = tc * kSymTile + tx * VN;
+    T xc[VN], colacc[VN];
 #pragma unroll
     for (int e = 0; e < VN; ++e) {
-      const long c = c0 + e;
-      // stored-triangle membership inside a diagonal tile
-      const bool in_row = !diag || (upper ? c >= r : c <= r);
-      const bool in_col = !diag || (upper ? c > r : c < r);
-      const T a = (r < n && c < n) ? av[e] : T(0);
-      if (in_row) rowacc = fma(a, xc[e], rowacc);
-      if (in_col) colacc[e] = fma(a, xr, colacc[e]);
+      xc[e] = c0e + e < n ? x[c0e + e] : T(0);
+      colacc[e] = T(0);
     }
+    const bool diag = tc == tr;
+    if (diag)
+      symv_tile<true, T, PASSES, VN, RPP>(av, xc, xr, rowacc, colacc, tx * VN, ty, upper);
+    else
+      symv_tile<false, T, PASSES, VN, RPP>(av, xc, xr, rowacc, colacc, tx * VN, ty, upper);
 #pragma unroll
-    for (int o = TPR / 2; o > 0; o >>= 1) rowacc += __shfl_xor_sync(0xffffffffu, rowacc, o);
-    if (tx == 0) rowsh[rr] = rowacc;
+    for (int e = 0; e < VN; ++e) colsh[ty][tx * VN + e] = colacc[e];
+    __syncthreads();
+    if (threadIdx.x < kSymTile) {
+      const int t = threadIdx.x;
+      T cs = 0;
+#pragma unroll
+      for (int q = 0; q < RPP; ++q) cs += colsh[q][t];
+      if (diag) {
+        diagcol[t] = cs;
+      } else {
+        const long rcol = tc * kSymTile + t;  // output rows of the tile's columns
+        if (rcol < n) P[tr * n + rcol] = cs;
+      }
+      const long rrow = tr * kSymTile + t;
+      if (tc != c0 && rrow < n) P[tc * n + rrow] = T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PASSES; ++p)
+#pragma unroll
+      for (int e = 0; e < VN; ++e) av[p][e] = an[p][e];
   }
+  // the strip's row sums: per row, the TPR per-thread partials in order
 #pragma unroll
-  for (int e = 0; e < VN; ++e) colsh[ty][tx * VN + e] = colacc[e];
+  for (int p = 0; p < PASSES; ++p) rowpart[ty + p * RPP][tx] = rowacc[p];
   __syncthreads();
   if (threadIdx.x < kSymTile) {
     const int t = threadIdx.x;
-    T cs = 0;
-#pragma unroll 4
-    for (int q = 0; q < RPP; ++q) cs += colsh[q][t];
-    const long rrow = tr * kSymTile + t;  // output rows of the stored tile's rows
-    const long rcol = tc * kSymTile + t;  // output rows of the stored tile's cols
-    if (diag) {
-      if (rrow < n) P[tc * n + rrow] = rowsh[t] + cs;
-    } else {
-      if (rrow < n) P[tc * n + rrow] = rowsh[t];
-      if (rcol < n) P[tr * n + rcol] = cs;
-    }
+    T rs = 0;
+#pragma unroll
+    for (int q = 0; q < TPR; ++q) rs += rowpart[t][q];
+    const long rrow = tr * kSymTile + t;
+    if (rrow < n) P[c0 * n + rrow] = rs + diagcol[t];
   }
 }
 
@@ -347,12 +397,12 @@ void symv(bool upper, long n, T alpha, const T *A, long lda, const T *x, long in
   cv.alloc();
   const T *xu = unit_view(n, x, incx, cv.at<T>(ox));
   T *P = cv.at<T>(op);
-  const long tiles = nt * (nt + 1) / 2;
+  const long grid = nt * ceil_div(nt, long(kSymStrip));
   if (vec_ok(A, lda))
-    symv_tile_kernel<T, true><<<unsigned(tiles), kThreads, 0, ctx().stream>>>(n, A, lda, xu, P, upper);
+    symv_strip_kernel<T, true><<<unsigned(grid), kThreads, 0, ctx().stream>>>(n, nt, A, lda, xu, P, upper);
   else
-    symv_tile_kernel<T, false><<<unsigned(tiles), kThreads, 0, ctx().stream>>>(n, A, lda, xu, P, upper);
-  EXB_LAUNCH("symv tile kernel");
+    symv_strip_kernel<T, false><<<unsigned(grid), kThreads, 0, ctx().stream>>>(n, nt, A, lda, xu, P, upper);
+  EXB_LAUNCH("symv strip kernel");
   count_launch();
   launch_finish<T, 0>(n, int(nt), P, alpha, beta, y, incy, nullptr, false);
 }
