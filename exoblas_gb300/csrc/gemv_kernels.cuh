@@ -32,8 +32,16 @@ __global__ void __launch_bounds__(kThreads)
   const int sub = lane % G;
   const long warp_global = (long(blockIdx.x) * kThreads + threadIdx.x) / 32;
   const long nwarps = long(gridDim.x) * (kThreads / 32);
-  for (long base = warp_global * RPW; base < rows; base += nwarps * RPW) {
-    const long i = base + lane / G;
+  long pass = 0;
+  for (long base = warp_global * RPW; base < rows; base += nwarps * RPW, ++pass) {
+    long i = base + lane / G;
+    if (tri != 0 && (pass & 1)) {
+      // triangle rows snake: odd passes over the rows run mirrored, so a
+      // warp's short and long rows pair up and every warp gets equal work
+      const long cs = pass * nwarps * RPW;
+      const long ce = cs + nwarps * RPW < rows ? cs + nwarps * RPW : rows;
+      i = i < ce ? ce - 1 - (i - cs) : rows;
+    }
     T acc = 0;
     if (i < rows) {
       long lo = 0, hi = cols;

@@ -173,7 +173,15 @@ __global__ void __launch_bounds__(kThreads)
                 int tri) {
   using V = typename V16<T>::type;
   constexpr int VN = V16<T>::N;
-  for (long i = blockIdx.x; i < rows; i += gridDim.x) {
+  long pass = 0;
+  for (long q = blockIdx.x; q < rows; q += gridDim.x, ++pass) {
+    long i = q;
+    if (tri != 0 && (pass & 1)) {
+      // triangle rows snake (odd passes mirrored) for equal work per CTA
+      const long cs = pass * gridDim.x;
+      const long ce = cs + gridDim.x < rows ? cs + gridDim.x : rows;
+      i = ce - 1 - (q - cs);
+    }
     long lo = 0, hi = cols;
     if (tri == 1) hi = i + 1;  // lower
     if (tri == 2) lo = i;      // upper
@@ -182,7 +190,8 @@ __global__ void __launch_bounds__(kThreads)
     const T ay = MODE == 2 ? alpha * y[i] : T(0);  // syr2.py:25-27
     const T *u = MODE == 1 ? x : y;
     auto upd = [&](T av, long j) -> T {
-      if (MODE == 2) return av + (ax * y[j] + ay * x[j]);
+      // two FMAs per element: the FP64 pipe, not HBM, bounds dsyr2 on GB300
+      if (MODE == 2) return fma(ay, x[j], fma(ax, y[j], av));
       return av + ax * u[j];
     };
     if (VEC) {
@@ -253,7 +262,7 @@ void syr2(bool upper, long n, T alpha, const T *x, long incx, const T *y, long i
 // src/level2/symv.py:10-35.  The stored triangle is cut into 64 x 64 tiles;
 // a CTA walks a strip of kSymStrip consecutive tiles of one storage tile
 // row, reading each tile once: the tile's row contribution (A_t x_cols)
-// accumulates across the strip in shared memory, its column contribution
+// accumulates across the strip in registers, its column contribution
 // (A_t^T x_rows, off-diagonal tiles) is written at once.  Output row tile r
 // receives one contribution per tile index c (slot c): P[c][rows of r]; a
 // strip's row sum goes to the slot of its first tile and its other slots
