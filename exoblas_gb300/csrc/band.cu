@@ -144,12 +144,11 @@ __global__ void __launch_bounds__(Tile<T>::kTR)
       long b0 = (lo_in + kPer - 1) / kPer * kPer, b1 = hi_in / kPer * kPer;
       const bool a16 = (reinterpret_cast<uintptr_t>(a) & 15u) == 0;
       if (!a16 || b1 < b0) b0 = b1 = lo_in;  // no aligned body: element copies only
-      for (long e = s0 + threadIdx.x; e < s1; e += kTR) {
-        if (e < lo_in || e >= hi_in)
-          tb[e - s0] = T(0);
-        else if (e < b0 || e >= b1)
-          cp_async_elem(&tb[e - s0], a + e);
-      }
+      // zeros outside the storage, element copies for the unaligned ends
+      for (long e = s0 + threadIdx.x; e < lo_in; e += kTR) tb[e - s0] = T(0);
+      for (long e = (hi_in > s0 ? hi_in : s0) + threadIdx.x; e < s1; e += kTR) tb[e - s0] = T(0);
+      for (long e = lo_in + threadIdx.x; e < b0; e += kTR) cp_async_elem(&tb[e - s0], a + e);
+      for (long e = b1 + threadIdx.x; e < hi_in; e += kTR) cp_async_elem(&tb[e - s0], a + e);
       for (long c = b0 + long(threadIdx.x) * kPer; c < b1; c += long(kTR) * kPer)
         cp_async_16(&tb[c - s0], a + c);
     } else {

@@ -55,6 +55,27 @@ struct Key<double> {
   static __device__ __forceinline__ double value(U k) { return __longlong_as_double((long long)k); }
 };
 
+// 32-bit magnitude keys for nrm2's range check: the FP32 key itself; for
+// FP64 the high word of |x| with bit 0 set when the low word is nonzero, so
+// a NaN whose payload lies in the low word still sorts above the infinity.
+// Keys order like the magnitudes up to the low word, which the range check
+// does not need.  (A 64-bit key max per element doubled dnrm2's FP64-pipe
+// time on GB300.)
+template <typename T>
+struct Mag32;
+template <>
+struct Mag32<float> {
+  static __device__ __forceinline__ unsigned of(float x) { return Key<float>::of(x); }
+  static __device__ __forceinline__ double value(unsigned k) { return Key<float>::value(k); }
+};
+template <>
+struct Mag32<double> {
+  static __device__ __forceinline__ unsigned of(double x) {
+    return (unsigned(__double2hiint(x)) & 0x7fffffffu) | unsigned(__double2loint(x) != 0);
+  }
+  static __device__ __forceinline__ double value(unsigned k) { return __hiloint2double(int(k), 0); }
+};
+
 // sum of squares: FP32 inputs through exact products p + e (e = fma(x, x, -p))
 // accumulated with TwoSum in an FP32 pair (no FP64 work per element); FP64
 // inputs with one FP64 FMA per element.  The largest magnitude is kept as
@@ -157,15 +178,14 @@ __device__ __forceinline__ void for_each(long n, const T *__restrict__ x, long i
 template <typename T>
 __global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ x, long inc, bool vec,
                                                   Part2 *partials, unsigned *counter, T *result, int *flag) {
-  using K = Key<T>;
+  using K = Mag32<T>;
   __shared__ Part2 sh[kT / 32];
   __shared__ bool last;
   SumSq<T> acc[kU];
-  typename K::U mk = 0;
+  unsigned mk = 0;
   for_each(n, x, inc, vec, [&](int u, T v, long) {
     acc[u].add(v);
-    const typename K::U k = K::of(v);
-    mk = k > mk ? k : mk;
+    mk = max(mk, K::of(v));
   });
   double ss = 0.0;
 #pragma unroll
@@ -262,11 +282,27 @@ __global__ void __launch_bounds__(kT) iamax_kernel(long n, const T *__restrict__
   __shared__ bool last;
   // keys are stored + 1 so that 0 means "none yet"; NaN keys never enter
   Best<U> accs[kU];
+  unsigned acc_hi[kU];  // FP64: high word of the slot's best magnitude
 #pragma unroll
-  for (int u = 0; u < kU; ++u) accs[u] = Best<U>{0, LONG_MAX};
+  for (int u = 0; u < kU; ++u) {
+    accs[u] = Best<U>{0, LONG_MAX};
+    acc_hi[u] = 0;
+  }
   for_each(n, x, inc, vec, [&](int u, T v, long i) {
-    const U k = K::of(v) + 1;
-    if (k <= K::kInf + 1 && k > accs[u].k) accs[u] = Best<U>{k, i};  // per slot increasing i: the first stays
+    if constexpr (sizeof(T) == 8) {
+      // a 32-bit test on the high word first: a larger key needs a high word
+      // at least the best's, and the 64-bit compare runs only then
+      const unsigned hk = unsigned(__double2hiint(double(v))) & 0x7fffffffu;
+      if (hk < acc_hi[u]) return;
+      const U k = K::of(v) + 1;
+      if (k <= K::kInf + 1 && k > accs[u].k) {
+        accs[u] = Best<U>{k, i};
+        acc_hi[u] = hk;
+      }
+    } else {
+      const U k = K::of(v) + 1;
+      if (k <= K::kInf + 1 && k > accs[u].k) accs[u] = Best<U>{k, i};  // per slot increasing i: the first stays
+    }
   });
   Best<U> acc = accs[0];
 #pragma unroll
