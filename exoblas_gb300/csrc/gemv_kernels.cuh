@@ -167,18 +167,54 @@ __global__ void __launch_bounds__(kThreads)
 
 // MODE 0: y_j = alpha * sum_c partial[c][j] + beta * y_j (gemv T, symv)
 // MODE 1: y_j = sum_c partial[c][j] (+ xs_j when unit)  (trmv T)
+// A CTA (kThreads) takes 32 consecutive j at a time: warp w sums slots
+// [w*chunks/8, (w+1)*chunks/8) in order, and the 8 warp sums are added in
+// warp order, so the result depends only on `chunks`.
+constexpr int kFinishCols = 32;
 template <typename T, int MODE>
-__global__ void finish_kernel(long cols, int chunks, const T *__restrict__ partial, T alpha, T beta, T *y, long incy,
-                              const T *xs, bool unit) {
-  for (long j = long(blockIdx.x) * blockDim.x + threadIdx.x; j < cols; j += long(gridDim.x) * blockDim.x) {
+__global__ void __launch_bounds__(kThreads)
+    finish_kernel(long cols, int chunks, const T *__restrict__ partial, T alpha, T beta, T *y, long incy,
+                  const T *xs, bool unit) {
+  constexpr int kW = kThreads / 32;
+  __shared__ T sh[kW][kFinishCols];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c0 = int(long(chunks) * w / kW), c1 = int(long(chunks) * (w + 1) / kW);
+  for (long g = blockIdx.x; g * kFinishCols < cols; g += gridDim.x) {
+    const long j = g * kFinishCols + lane;
     T s = 0;
-    for (int c = 0; c < chunks; ++c) s += partial[long(c) * cols + j];
-    T *yj = y + j * incy;
-    if (MODE == 0)
-      *yj = alpha * s + beta * *yj;
-    else
-      *yj = unit ? s + xs[j] : s;
+    if (j < cols) {
+      int c = c0;
+      for (; c + 3 < c1; c += 4) {
+        const T p0 = partial[long(c) * cols + j], p1 = partial[long(c + 1) * cols + j],
+                p2 = partial[long(c + 2) * cols + j], p3 = partial[long(c + 3) * cols + j];
+        s += p0;
+        s += p1;
+        s += p2;
+        s += p3;
+      }
+      for (; c < c1; ++c) s += partial[long(c) * cols + j];
+    }
+    sh[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && j < cols) {
+      T t = 0;
+#pragma unroll
+      for (int q = 0; q < kW; ++q) t += sh[q][lane];
+      T *yj = y + j * incy;
+      if (MODE == 0)
+        *yj = alpha * t + beta * *yj;
+      else
+        *yj = unit ? t + xs[j] : t;
+    }
+    __syncthreads();
   }
+}
+
+// CTAs for finish_kernel over `cols` outputs, at most `cap`
+inline long finish_blocks(long cols, long cap) {
+  long b = (cols + kFinishCols - 1) / kFinishCols;
+  if (b > cap) b = cap;
+  return b < 1 ? 1 : b;
 }
 
 }  // namespace l2

@@ -108,8 +108,7 @@ static void launch_colsum(long rows, long cols, const T *A, long lda, const T *x
 template <typename T, int MODE>
 static void launch_finish(long cols, int chunks, const T *partial, T alpha, T beta, T *y, long incy, const T *xs,
                           bool unit) {
-  long blocks = ceil_div(cols, kThreads);
-  if (blocks > grid_cap(4)) blocks = grid_cap(4);
+  const long blocks = finish_blocks(cols, grid_cap(8));
   finish_kernel<T, MODE><<<int(blocks), kThreads, 0, ctx().stream>>>(cols, chunks, partial, alpha, beta, y, incy, xs,
                                                                      unit);
   EXB_LAUNCH("partial-sum kernel");

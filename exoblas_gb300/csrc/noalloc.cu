@@ -100,8 +100,7 @@ static void sgemv_noalloc(int order, int TransA, int M, int N, float alpha, cons
   if (xlen == 0) {
     // y = beta * y (gemv.py:13-14): the finish kernel with no partial sums
     if (!on_device(Y)) fail(EXOBLAS_INVALID_VALUE, "exoblas_sgemv_noalloc takes device pointers only");
-    long blocks = ceil_div(ylen, l2::kThreads);
-    if (blocks > long(d.sm_count) * 4) blocks = long(d.sm_count) * 4;
+    const long blocks = l2::finish_blocks(ylen, long(d.sm_count) * 8);
     l2::finish_kernel<float, 0><<<int(blocks), l2::kThreads, 0, stream>>>(ylen, 0, nullptr, alpha, beta, Y, incY,
                                                                          nullptr, false);
     EXB_LAUNCH("partial-sum kernel");
@@ -171,8 +170,7 @@ static void sgemv_noalloc(int order, int TransA, int M, int N, float alpha, cons
     else
       colsum_kernel<float, false><<<grid, kThreads, 0, stream>>>(rows, cols, A, lda, xu, rpc, partial, 0, false);
     EXB_LAUNCH("column-sum kernel");
-    long blocks = ceil_div(cols, kThreads);
-    if (blocks > long(d.sm_count) * 4) blocks = long(d.sm_count) * 4;
+    const long blocks = finish_blocks(cols, long(d.sm_count) * 8);
     finish_kernel<float, 0><<<int(blocks), kThreads, 0, stream>>>(cols, chunks, partial, alpha, beta, Y, incY, nullptr,
                                                                  false);
     EXB_LAUNCH("partial-sum kernel");
