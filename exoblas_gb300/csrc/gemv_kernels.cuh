@@ -57,17 +57,32 @@ __global__ void __launch_bounds__(kThreads)
         const V *xv = reinterpret_cast<const V *>(x);
         long v = vlo / VN + sub;
         const long ve = vhi / VN;
-        for (; v + 3 * G < ve; v += 4 * G) {
-          V a0 = ld_stream(av + v), a1 = ld_stream(av + v + G), a2 = ld_stream(av + v + 2 * G),
-            a3 = ld_stream(av + v + 3 * G);
-          V x0 = xv[v], x1 = xv[v + G], x2 = xv[v + 2 * G], x3 = xv[v + 3 * G];
+        // software pipeline: the row's next 4 vectors are loaded before the
+        // current 4 are consumed (x comes from L1/L2 at use)
+        V ra[4], rn[4];
+        bool have = v + 3 * G < ve;
+        if (have) {
 #pragma unroll
-          for (int e = 0; e < VN; ++e) {
-            acc = fma(vget<T>(a0, e), vget<T>(x0, e), acc);
-            acc = fma(vget<T>(a1, e), vget<T>(x1, e), acc);
-            acc = fma(vget<T>(a2, e), vget<T>(x2, e), acc);
-            acc = fma(vget<T>(a3, e), vget<T>(x3, e), acc);
+          for (int u = 0; u < 4; ++u) ra[u] = ld_stream(av + v + u * G);
+        }
+        while (have) {
+          const long vn = v + 4 * G;
+          const bool more = vn + 3 * G < ve;
+          if (more) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) rn[u] = ld_stream(av + vn + u * G);
           }
+          V xr[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) xr[u] = xv[v + u * G];
+#pragma unroll
+          for (int e = 0; e < VN; ++e)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc = fma(vget<T>(ra[u], e), vget<T>(xr[u], e), acc);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) ra[u] = rn[u];
+          v = vn;
+          have = more;
         }
         for (; v < ve; v += G) {
           V a0 = ld_stream(av + v), x0 = xv[v];

@@ -314,17 +314,40 @@ __global__ void __launch_bounds__(kThreads)
     const V *xv = reinterpret_cast<const V *>(x + head);
     const V *yv = reinterpret_cast<const V *>(y + head);
     long v = gt;
-    for (; v + (kUnroll - 1) * stride < nvec; v += kUnroll * stride) {
-      V a[kUnroll], b[kUnroll];
+    // software pipeline: the next kU vectors (of x and y) are loaded
+    // before the current ones are consumed; one-operand reductions keep
+    // twice as many vectors per thread in flight
+    constexpr int kU = Acc::TWO ? kUnroll : 2 * kUnroll;
+    V a[kU], b[kU], na[kU], nb[kU];
+    bool have = v + (kU - 1) * stride < nvec;
+    if (have) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u) {
+      for (int u = 0; u < kU; ++u) {
         a[u] = ld_stream(xv + v + u * stride);
         if (Acc::TWO) b[u] = ld_stream(yv + v + u * stride);
       }
+    }
+    while (have) {
+      const long vn = v + kU * stride;
+      const bool more = vn + (kU - 1) * stride < nvec;
+      if (more) {
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
+        for (int u = 0; u < kU; ++u) {
+          na[u] = ld_stream(xv + vn + u * stride);
+          if (Acc::TWO) nb[u] = ld_stream(yv + vn + u * stride);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
 #pragma unroll
         for (int e = 0; e < VN; ++e) acc.add(vget<T>(a[u], e), Acc::TWO ? vget<T>(b[u], e) : T(0));
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        a[u] = na[u];
+        if (Acc::TWO) b[u] = nb[u];
+      }
+      v = vn;
+      have = more;
     }
     for (; v < nvec; v += stride) {
       V a = ld_stream(xv + v), b;
@@ -391,7 +414,9 @@ void run_reduce(long n, const typename Acc::In *x, long incx, const typename Acc
   long work = unit ? (n / VN) : n;
   long blocks = ceil_div(work, long(kThreads) * kUnroll);
   if (blocks < 1) blocks = 1;
-  if (blocks > grid_cap(4)) blocks = grid_cap(4);
+  // one wave of resident CTAs at most
+  const int per_sm = resident_per_sm(reinterpret_cast<const void *>(reduce_kernel<Acc>), kThreads);
+  if (blocks > grid_cap(per_sm < 4 ? per_sm : 4)) blocks = grid_cap(per_sm < 4 ? per_sm : 4);
   P *partials = static_cast<P *>(scratch(sizeof(P) * blocks));
   unsigned int *counter = zero_words(1);
   reduce_kernel<Acc><<<int(blocks), kThreads, 0, s>>>(n, x, incx, y, incy, head, unit, partials, counter, result, sb,
