@@ -316,36 +316,38 @@ __global__ void __launch_bounds__(kThreads)
     long v = gt;
     // software pipeline: the next kU vectors (of x and y) are loaded
     // before the current ones are consumed; one-operand reductions keep
-    // twice as many vectors per thread in flight
+    // twice as many vectors per thread in flight.  Two register buffers
+    // alternate (the body is written twice), so no vector is copied between
+    // registers; measured faster than copying the prefetched buffer (ddot
+    // 0.90 -> 0.95 of the HBM copy bandwidth on GB300).
     constexpr int kU = Acc::TWO ? kUnroll : 2 * kUnroll;
-    V a[kU], b[kU], na[kU], nb[kU];
-    bool have = v + (kU - 1) * stride < nvec;
-    if (have) {
+    V a0[kU], b0[kU], a1[kU], b1[kU];
+    auto load = [&](V(&xa)[kU], V(&ya)[kU], long at) {
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
-        a[u] = ld_stream(xv + v + u * stride);
-        if (Acc::TWO) b[u] = ld_stream(yv + v + u * stride);
+        xa[u] = ld_stream(xv + at + u * stride);
+        if (Acc::TWO) ya[u] = ld_stream(yv + at + u * stride);
       }
-    }
-    while (have) {
-      const long vn = v + kU * stride;
-      const bool more = vn + (kU - 1) * stride < nvec;
-      if (more) {
-#pragma unroll
-        for (int u = 0; u < kU; ++u) {
-          na[u] = ld_stream(xv + vn + u * stride);
-          if (Acc::TWO) nb[u] = ld_stream(yv + vn + u * stride);
-        }
-      }
+    };
+    auto use = [&](V(&xa)[kU], V(&ya)[kU]) {
 #pragma unroll
       for (int u = 0; u < kU; ++u)
 #pragma unroll
-        for (int e = 0; e < VN; ++e) acc.add(vget<T>(a[u], e), Acc::TWO ? vget<T>(b[u], e) : T(0));
-#pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        a[u] = na[u];
-        if (Acc::TWO) b[u] = nb[u];
-      }
+        for (int e = 0; e < VN; ++e) acc.add(vget<T>(xa[u], e), Acc::TWO ? vget<T>(ya[u], e) : T(0));
+    };
+    bool have = v + (kU - 1) * stride < nvec;
+    if (have) load(a0, b0, v);
+    while (have) {
+      long vn = v + kU * stride;
+      bool more = vn + (kU - 1) * stride < nvec;
+      if (more) load(a1, b1, vn);
+      use(a0, b0);
+      v = vn;
+      if (!more) break;
+      vn = v + kU * stride;
+      more = vn + (kU - 1) * stride < nvec;
+      if (more) load(a0, b0, vn);
+      use(a1, b1);
       v = vn;
       have = more;
     }

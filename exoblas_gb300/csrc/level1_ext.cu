@@ -125,6 +125,100 @@ __device__ __forceinline__ Part2 part2_reduce_block(Part2 v, Part2 *sh) {
   return r;  // valid in thread 0
 }
 
+// The vector loop of for_each with index type I: 32-bit when the vector
+// count allows it, 64-bit otherwise.
+template <typename I, typename T, class F>
+__device__ __forceinline__ void for_each_vec(I nvec, const typename V16<T>::type *__restrict__ xv, I gt, I stride,
+                                             F &f) {
+  using V = typename V16<T>::type;
+  constexpr int VN = V16<T>::N;
+  I v = gt;
+  // the next kU vectors are loaded before the current ones are consumed
+  V a[kU], b[kU];
+  bool have = v + (kU - 1) * stride < nvec;
+  if (have) {
+#pragma unroll
+    for (int u = 0; u < kU; ++u) a[u] = ld_stream(xv + v + u * stride);
+  }
+  while (have) {
+    const I vn = v + kU * stride;
+    const bool more = vn + (kU - 1) * stride < nvec;
+    if (more) {
+#pragma unroll
+      for (int u = 0; u < kU; ++u) b[u] = ld_stream(xv + vn + u * stride);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u)
+#pragma unroll
+      for (int e = 0; e < VN; ++e) f(u, vget<T>(a[u], e), long(v + u * stride) * VN + e);
+#pragma unroll
+    for (int u = 0; u < kU; ++u) a[u] = b[u];
+    v = vn;
+    have = more;
+  }
+  for (; v < nvec; v += stride) {
+    const V c = ld_stream(xv + v);
+#pragma unroll
+    for (int e = 0; e < VN; ++e) f(0, vget<T>(c, e), long(v) * VN + e);
+  }
+}
+
+// FP64 data as 32-bit words: calls f(slot, hi, lo, index) for each element
+// (hi and lo the words of its bit pattern), with the pipelined loop of
+// for_each_vec over 16-byte vectors of two elements.  The buffers hold no
+// FP64 values: with double2 buffers idamax kept GB300's FP64 pipe 72% busy
+// without a single FP64 arithmetic instruction; with these it is idle.
+template <typename I, class F>
+__device__ __forceinline__ void for_each_words(I nvec, const uint4 *__restrict__ xv, I gt, I stride, F &f) {
+  I v = gt;
+  uint4 a[kU], b[kU];
+  bool have = v + (kU - 1) * stride < nvec;
+  if (have) {
+#pragma unroll
+    for (int u = 0; u < kU; ++u) a[u] = ld_stream(xv + v + u * stride);
+  }
+  while (have) {
+    const I vn = v + kU * stride;
+    const bool more = vn + (kU - 1) * stride < nvec;
+    if (more) {
+#pragma unroll
+      for (int u = 0; u < kU; ++u) b[u] = ld_stream(xv + vn + u * stride);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      f(u, a[u].y, a[u].x, long(v + u * stride) * 2);
+      f(u, a[u].w, a[u].z, long(v + u * stride) * 2 + 1);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) a[u] = b[u];
+    v = vn;
+    have = more;
+  }
+  for (; v < nvec; v += stride) {
+    const uint4 c = ld_stream(xv + v);
+    f(0, c.y, c.x, long(v) * 2);
+    f(0, c.w, c.z, long(v) * 2 + 1);
+  }
+}
+
+// for_each for FP64 data as words: f(slot, hi, lo, index)
+template <class F>
+__device__ __forceinline__ void words(long n, const double *__restrict__ x, long inc, bool vec, F &f) {
+  const long stride = long(gridDim.x) * kT, gt = long(blockIdx.x) * kT + threadIdx.x;
+  auto one = [&](double d, long i) { f(0, unsigned(__double2hiint(d)), unsigned(__double2loint(d)), i); };
+  if (vec) {
+    const long nvec = n / 2;
+    const uint4 *xv = reinterpret_cast<const uint4 *>(x);
+    if (nvec + 2 * kU * stride < (1L << 32))
+      for_each_words<unsigned>(unsigned(nvec), xv, unsigned(gt), unsigned(stride), f);
+    else
+      for_each_words<long>(nvec, xv, gt, stride, f);
+    for (long i = nvec * 2 + gt; i < n; i += stride) one(x[i], i);
+  } else {
+    for (long i = gt; i < n; i += stride) one(x[i * inc], i);
+  }
+}
+
 // Calls f(slot, value, index) for this thread's elements: 16-byte vectors
 // when x is unit-stride and aligned, kU of them consumed per step while the
 // next kU are in flight; slot u < kU names an independent accumulator (the
@@ -138,35 +232,12 @@ __device__ __forceinline__ void for_each(long n, const T *__restrict__ x, long i
   if (vec) {
     const long nvec = n / VN;
     const V *xv = reinterpret_cast<const V *>(x);
-    long v = gt;
-    // the next kU vectors are loaded before the current ones are consumed
-    V a[kU], b[kU];
-    bool have = v + (kU - 1) * stride < nvec;
-    if (have) {
-#pragma unroll
-      for (int u = 0; u < kU; ++u) a[u] = ld_stream(xv + v + u * stride);
-    }
-    while (have) {
-      const long vn = v + kU * stride;
-      const bool more = vn + (kU - 1) * stride < nvec;
-      if (more) {
-#pragma unroll
-        for (int u = 0; u < kU; ++u) b[u] = ld_stream(xv + vn + u * stride);
-      }
-#pragma unroll
-      for (int u = 0; u < kU; ++u)
-#pragma unroll
-        for (int e = 0; e < VN; ++e) f(u, vget<T>(a[u], e), (v + u * stride) * VN + e);
-#pragma unroll
-      for (int u = 0; u < kU; ++u) a[u] = b[u];
-      v = vn;
-      have = more;
-    }
-    for (; v < nvec; v += stride) {
-      const V c = ld_stream(xv + v);
-#pragma unroll
-      for (int e = 0; e < VN; ++e) f(0, vget<T>(c, e), v * VN + e);
-    }
+    // 32-bit indices while every index the loop forms (up to nvec plus
+    // 2 kU strides) stays below 2^32
+    if (nvec + 2 * kU * stride < (1L << 32))
+      for_each_vec<unsigned, T>(unsigned(nvec), xv, unsigned(gt), unsigned(stride), f);
+    else
+      for_each_vec<long, T>(nvec, xv, gt, stride, f);
     for (long i = nvec * VN + gt; i < n; i += stride) f(0, x[i], i);
   } else {
     for (long i = gt; i < n; i += stride) f(0, x[i * inc], i);
@@ -288,22 +359,26 @@ __global__ void __launch_bounds__(kT) iamax_kernel(long n, const T *__restrict__
     accs[u] = Best<U>{0, LONG_MAX};
     acc_hi[u] = 0;
   }
-  for_each(n, x, inc, vec, [&](int u, T v, long i) {
-    if constexpr (sizeof(T) == 8) {
-      // a 32-bit test on the high word first: a larger key needs a high word
-      // at least the best's, and the 64-bit compare runs only then
-      const unsigned hk = unsigned(__double2hiint(double(v))) & 0x7fffffffu;
+  if constexpr (sizeof(T) == 8) {
+    // FP64: the elements as 32-bit words; a test on the high word first (a
+    // larger key needs a high word at least the best's), the 64-bit key only
+    // then
+    auto upd = [&](int u, unsigned hi, unsigned lo, long i) {
+      const unsigned hk = hi & 0x7fffffffu;
       if (hk < acc_hi[u]) return;
-      const U k = K::of(v) + 1;
-      if (k <= K::kInf + 1 && k > accs[u].k) {
+      const U k = ((U(hk) << 32) | lo) + 1;
+      if (k <= K::kInf + 1 && k > accs[u].k) {  // per slot increasing i: the first stays
         accs[u] = Best<U>{k, i};
         acc_hi[u] = hk;
       }
-    } else {
+    };
+    words(n, x, inc, vec, upd);
+  } else {
+    for_each(n, x, inc, vec, [&](int u, T v, long i) {
       const U k = K::of(v) + 1;
       if (k <= K::kInf + 1 && k > accs[u].k) accs[u] = Best<U>{k, i};  // per slot increasing i: the first stays
-    }
-  });
+    });
+  }
   Best<U> acc = accs[0];
 #pragma unroll
   for (int u = 1; u < kU; ++u) acc = better(acc, accs[u]);
