@@ -22,6 +22,8 @@ roofline   the kernel with the largest share of the step, against the
            measured HBM copy bandwidth in MEASURED_PEAKS.json.
 cpu_baseline  the CPU oracle (C++ restatement of the reference algorithms,
            threaded over ranges/rows) on a bounded sample of the same set.
+cpu_openblas  the same sample through SciPy's bundled OpenBLAS, the CBLAS
+           the reference compares against: one thread and all host threads.
 
 --impl reference times that CPU implementation alone on the host cores.
 Multi-GPU: replicas only (one independent replica per rank, no collective).
@@ -219,8 +221,9 @@ SAMPLE = {  # bounded CPU sample of the same set (sizes divided down)
     "saxpy": 1 << 24, "sdot": 1 << 24, "dsdot": 1 << 24, "daxpy": 1 << 23, "ddot": 1 << 23,
     "sgemv_n": 8192, "sgemv_t": 8192, "dtrsv": 4096,
 }
-SAMPLE_DESC = ("same set at reduced sizes: saxpy/sdot/dsdot n=2^24, daxpy/ddot n=2^23, sgemv N+T 8192^2, "
-               "dtrsv n=4096; oracle_par_* drivers (C++ restatement of the reference algorithms, -O3)")
+SAMPLE_SIZES = ("same set at reduced sizes: saxpy/sdot/dsdot n=2^24, daxpy/ddot n=2^23, sgemv N+T 8192^2, "
+                "dtrsv n=4096")
+SAMPLE_DESC = SAMPLE_SIZES + "; oracle_par_* drivers (C++ restatement of the reference algorithms, -O3)"
 
 
 def sample_bytes(k):
@@ -293,6 +296,56 @@ def cpu_baseline(min_seconds=10.0):
         reps += 1
     return {"value": total_b / total_t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{SAMPLE_DESC}; {reps} passes, {total_t:.1f} s"}
+
+
+def openblas_step(S):
+    """One pass of the CPU sample through SciPy's bundled OpenBLAS (the CBLAS
+    the reference compares against); returns per-kernel seconds."""
+    from oracle import cblas
+
+    t = {}
+    for k in SAMPLE:
+        n = SAMPLE[k]
+        a = S[k]
+        t0 = time.perf_counter()
+        if k in ("saxpy", "daxpy"):
+            cblas.call(k, n, 0.75, a[0], 1, a[1], 1)
+        elif k in ("sdot", "ddot", "dsdot"):
+            cblas.call(k, n, a[0], 1, a[1], 1)
+        elif k in ("sgemv_n", "sgemv_t"):
+            cblas.call("sgemv", 101, 111 if k == "sgemv_n" else 112, n, n, 1.0, a[0], n, a[1], 1, 0.5, a[2], 1)
+        elif k == "dtrsv":
+            x = a[1].copy()
+            cblas.call("dtrsv", 101, 122, 111, 131, n, a[0], n, x, 1)
+        t[k] = time.perf_counter() - t0
+    return t
+
+
+def openblas_baseline(seconds_each=5.0):
+    """The same bounded sample as cpu_baseline through OpenBLAS, one thread
+    and all host threads (the reference's own comparison library)."""
+    try:
+        from oracle import cblas
+
+        if not cblas.available():
+            return {"unavailable": "SciPy's bundled OpenBLAS not found"}
+    except ImportError as e:
+        return {"unavailable": f"oracle.cblas: {e}"}
+    S = cpu_sample_inputs()
+    out = {"unit": UNIT, "kind": "OpenBLAS bundled with SciPy (scipy_cblas_*)", "sample": SAMPLE_SIZES}
+    cores = os.cpu_count() or 1
+    for label, threads in (("one_thread", 1), ("all_threads", cores)):
+        cblas.set_threads(threads)
+        openblas_step(S)  # warm-up
+        tb, tt = 0, 0.0
+        while tt < seconds_each:
+            t = openblas_step(S)
+            tt += sum(t.values())
+            tb += sum(sample_bytes(k) for k in SAMPLE)
+        out[label] = round(tb / tt / 1e9, 3)
+    out["cores"] = cores
+    cblas.set_threads(1)
+    return out
 
 
 # ------------------------------------------------------------------- main --
@@ -430,9 +483,10 @@ def main():
                "h2d_bytes_per_step": (h1.value - h0.value) // KE, "d2h_bytes_per_step": (d1.value - d0.value) // KE,
                "steps": KE}
 
-    cpu = None
+    cpu = openblas = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
+        openblas = openblas_baseline()
 
     if rank == 0:
         line = {
@@ -455,6 +509,7 @@ def main():
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / hbm, 3),
                          "traffic": traffic.get(dom)},
             "cpu_baseline": cpu,
+            "cpu_openblas": openblas,
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk,
