@@ -7,7 +7,8 @@ NumPy buffers filled the way the reference's AlignedBuffer fills them
 (1 + (N-1)|inc| elements, uniform[-1, 1), test/common/generate_buffer.h:
 12-78), but from a seeded PCG64 generator so runs reproduce.
 
-Checks, in the order the reference and the benchmark spec define them:
+Checks, in the order the reference and the project's accuracy contract
+define them:
 - the reference's own rule, |r - e| / max(1, |e|) < 1% on every element of
   every output buffer, padding included (test/common/correctness_helpers.h:
   9-16, generate_buffer.h:57-68);

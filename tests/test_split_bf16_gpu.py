@@ -3,8 +3,7 @@
 Each FP32 operand is carried as three BF16 terms; results must meet the same
 FP32 componentwise bound as the FFMA path (reference grids of
 test/level3/{gemm,symm,syrk}/correctness.cpp), and at larger sizes the max
-relative error against FP64 must be no worse than the plain FP32 path's
-(north star: "max relative error no worse than plain FP32 against FP64")."""
+relative error against FP64 must be no worse than the plain FP32 path's."""
 import numpy as np
 import pytest
 
