@@ -741,23 +741,79 @@ __global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
   __syncthreads();
   if (tid < kTB) rd[tid] = T(1) / L[tid][tid];
   __syncthreads();
-  const int c = tid >> 2, q = tid & 3;
-  const unsigned mask = 0xfu << ((threadIdx.x & 31) & ~3);
-  if (q == 0) Y[c][c] = rd[c];
-  __syncwarp(mask);
-  for (int i = c + 1; i < kTB; ++i) {
-    T s0 = 0, s1 = 0;
-    int j = c + q;
-    for (; j + 4 < i; j += 8) {
-      s0 = fma(L[i][j], Y[j][c], s0);
-      s1 = fma(L[i][j + 4], Y[j + 4][c], s1);
-    }
-    if (j < i) s0 = fma(L[i][j], Y[j][c], s0);
-    T s = s0 + s1;
-    s += __shfl_xor_sync(mask, s, 1);
-    s += __shfl_xor_sync(mask, s, 2);
-    if (q == 0) Y[i][c] = -s * rd[i];
+  // Blocked inverse: 16x16 leaves by substitution, then 32x32 and 64x64 by
+  // inv([A 0; B C]) = [inv(A) 0; -inv(C) B inv(A), inv(C)], the products
+  // taking the triangles into account.  The dependency chains are 16 steps
+  // instead of 64; the FMA count stays n^3/6.  The strictly upper 32x32
+  // block of L (zeros, never read) holds the products' scratch:
+  // W(i, j) = L[i][32 + j].
+  {
+    // leaves: four 16x16 blocks, 64 threads each, 4 lanes per column
+    const int o = (tid >> 6) * 16, c = (tid & 63) >> 2, q = tid & 3;
+    const unsigned mask = 0xfu << ((threadIdx.x & 31) & ~3);
+    if (q == 0) Y[o + c][o + c] = rd[o + c];
     __syncwarp(mask);
+    for (int i = c + 1; i < 16; ++i) {
+      T s = 0;
+      for (int j = c + q; j < i; j += 4) s = fma(L[o + i][o + j], Y[o + j][o + c], s);
+      s += __shfl_xor_sync(mask, s, 1);
+      s += __shfl_xor_sync(mask, s, 2);
+      if (q == 0) Y[o + i][o + c] = -s * rd[o + i];
+      __syncwarp(mask);
+    }
+  }
+  __syncthreads();
+  // 32x32 blocks p = 0, 1 at P = 32p:
+  //   W = L[P+16.., P..] inv(A)     W(i, j) = sum_{k=j..15} L[P+16+i][P+k] Y[P+k][P+j]
+  {
+    const int P = (tid >> 7) * 32, u = tid & 127, i = u >> 3, jq = u & 7;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = h ? 15 - jq : jq;  // column pairs of equal total length
+      T s = 0;
+      for (int k = j; k < 16; ++k) s = fma(L[P + 16 + i][P + k], Y[P + k][P + j], s);
+      L[(P >> 1) + i][32 + j] = s;
+    }
+  }
+  __syncthreads();
+  //   Y[P+16+i][P+j] = - sum_{k=0..i} Y[P+16+i][P+16+k] W(k, j)
+  {
+    const int P = (tid >> 7) * 32, u = tid & 127, ip = u >> 4, j = u & 15;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = h ? 15 - ip : ip;  // row pairs of equal total length
+      T s = 0;
+      for (int k = 0; k <= i; ++k) s = fma(Y[P + 16 + i][P + 16 + k], L[(P >> 1) + k][32 + j], s);
+      Y[P + 16 + i][P + j] = -s;
+    }
+  }
+  __syncthreads();
+  // 64x64: W = L[32.., 0..31] inv(A32)   W(i, j) = sum_{k=j..31} L[32+i][k] Y[k][j]
+  {
+    const int ip = tid >> 4, jq = tid & 15;
+#pragma unroll
+    for (int hi = 0; hi < 2; ++hi)
+#pragma unroll
+      for (int hj = 0; hj < 2; ++hj) {
+        const int i = hi ? 31 - ip : ip, j = hj ? 31 - jq : jq;
+        T s = 0;
+        for (int k = j; k < 32; ++k) s = fma(L[32 + i][k], Y[k][j], s);
+        L[i][32 + j] = s;
+      }
+  }
+  __syncthreads();
+  //   Y[32+i][j] = - sum_{k=0..i} Y[32+i][32+k] W(k, j)
+  {
+    const int ip = tid >> 4, jq = tid & 15;
+#pragma unroll
+    for (int hi = 0; hi < 2; ++hi)
+#pragma unroll
+      for (int hj = 0; hj < 2; ++hj) {
+        const int i = hi ? 31 - ip : ip, j = hj ? 31 - jq : jq;
+        T s = 0;
+        for (int k = 0; k <= i; ++k) s = fma(Y[32 + i][32 + k], L[k][32 + j], s);
+        Y[32 + i][j] = -s;
+      }
   }
   __syncthreads();
   T *out = const_cast<T *>(a.inv) + K * kTB * kTB;
