@@ -34,8 +34,6 @@ namespace ext {
 constexpr int kT = 256;
 constexpr int kU = 4;  // vectors in flight per thread
 
-__device__ __forceinline__ double nan_max(double a, double b) { return (b > a || b != b) ? b : a; }
-
 // magnitude keys: |x| as an unsigned bit pattern orders like |x| for every
 // non-NaN value, and every NaN's key is above the infinity's
 template <typename T>
@@ -102,27 +100,80 @@ struct SumSq<double> {
   __device__ __forceinline__ double get() const { return ss; }
 };
 
+// A per-CTA partial of nrm2: the sum of squares and the largest magnitude
+// as its 32-bit key (integer max all the way: NaN keys sort above the
+// infinity's, so a NaN anywhere survives the combination).
 struct Part2 {
-  double ss, mx;
+  double ss;
+  unsigned mk;
 };
 
-__device__ __forceinline__ Part2 part2_reduce_block(Part2 v, Part2 *sh) {
+// FP32 pairs (hi + lo) added with TwoSum: the FP32 path combines its slots
+// and lanes this way and converts to FP64 once per warp.  (Per-thread FP64
+// conversions and adds at the end of the stream kept GB300's slow FP64 pipe
+// 19% busy in snrm2.)
+struct F2 {
+  float hi, lo;
+};
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+  const float s = a.hi + b.hi;
+  const float z = s - a.hi;
+  const float e = ((a.hi - (s - z)) + (b.hi - z)) + (a.lo + b.lo);
+  const float hi = s + e;
+  return F2{hi, e - (hi - s)};
+}
+
+// Block combination in a fixed order: the warp tree, then thread 0 over
+// the warps.  Returns the total in thread 0.
+__device__ __forceinline__ Part2 part2_block(double ss, unsigned mk, Part2 *sh) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    v.ss += __shfl_xor_sync(0xffffffffu, v.ss, o);
-    v.mx = nan_max(v.mx, __shfl_xor_sync(0xffffffffu, v.mx, o));
+    ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
   }
-  if (lane == 0) sh[w] = v;
+  if (lane == 0) sh[w] = Part2{ss, mk};
   __syncthreads();
-  Part2 r{0.0, 0.0};
+  Part2 r{0.0, 0u};
   if (threadIdx.x == 0)
     for (int i = 0; i < kT / 32; ++i) {
       r.ss += sh[i].ss;
-      r.mx = nan_max(r.mx, sh[i].mx);
+      r.mk = max(r.mk, sh[i].mk);
     }
   __syncthreads();
-  return r;  // valid in thread 0
+  return r;
+}
+
+// The per-thread slots of a streaming pass, combined over the block.
+template <typename T>
+__device__ __forceinline__ Part2 sumsq_block(const SumSq<T> (&acc)[kU], unsigned mk, Part2 *sh) {
+  if constexpr (sizeof(T) == 4) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    F2 t{acc[0].hi, acc[0].lo};
+#pragma unroll
+    for (int u = 1; u < kU; ++u) t = f2_add(t, F2{acc[u].hi, acc[u].lo});
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const F2 other{__shfl_xor_sync(0xffffffffu, t.hi, o), __shfl_xor_sync(0xffffffffu, t.lo, o)};
+      t = f2_add(t, other);
+      mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+    }
+    if (lane == 0) sh[w] = Part2{double(t.hi) + double(t.lo), mk};
+    __syncthreads();
+    Part2 r{0.0, 0u};
+    if (threadIdx.x == 0)
+      for (int i = 0; i < kT / 32; ++i) {
+        r.ss += sh[i].ss;
+        r.mk = max(r.mk, sh[i].mk);
+      }
+    __syncthreads();
+    return r;
+  } else {
+    double ss = 0.0;
+#pragma unroll
+    for (int u = 0; u < kU; ++u) ss += acc[u].get();
+    return part2_block(ss, mk, sh);
+  }
 }
 
 // The vector loop of for_each with index type I: 32-bit when the vector
@@ -258,10 +309,7 @@ __global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ 
     acc[u].add(v);
     mk = max(mk, K::of(v));
   });
-  double ss = 0.0;
-#pragma unroll
-  for (int u = 0; u < kU; ++u) ss += acc[u].get();
-  Part2 tot = part2_reduce_block(Part2{ss, K::value(mk)}, sh);
+  Part2 tot = sumsq_block<T>(acc, mk, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = tot;
     __threadfence();
@@ -272,27 +320,28 @@ __global__ void __launch_bounds__(kT) nrm2_kernel(long n, const T *__restrict__ 
   __threadfence();
   // the last CTA combines the per-CTA partials: thread t takes CTAs t,
   // t + kT, ... in order, then the fixed block tree
-  Part2 mine{0.0, 0.0};
+  double ss = 0.0;
+  unsigned m = 0;
   for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) {
-    const Part2 p{__ldcg(&partials[b].ss), __ldcg(&partials[b].mx)};
-    mine.ss += p.ss;
-    mine.mx = nan_max(mine.mx, p.mx);
+    ss += __ldcg(&partials[b].ss);
+    m = max(m, __ldcg(&partials[b].mk));
   }
-  const Part2 g = part2_reduce_block(mine, sh);
+  const Part2 g = part2_block(ss, m, sh);
   if (threadIdx.x != 0) return;
   *counter = 0;
+  const double mx = K::value(g.mk);
   // squares and per-thread sums of up to 2^20 of them stay in range and
   // normal while the largest magnitude lies in [tiny, lim]
   const double lim = sizeof(T) == 8 ? 0x1p490 : 0x1p40, tiny = sizeof(T) == 8 ? 0x1p-490 : 0x1p-40;
   int e = 0;
-  if (g.mx == g.mx && g.mx != INFINITY && g.mx != 0.0 && (g.mx > lim || g.mx < tiny)) {
-    e = ilogb(g.mx);
+  if (mx == mx && mx != INFINITY && mx != 0.0 && (mx > lim || mx < tiny)) {
+    e = ilogb(mx);
     if (e == 0) e = 1;  // 0 means "no rescale"
   }
   *flag = e;
-  if (g.mx != g.mx)
-    *result = T(g.mx);  // NaN
-  else if (g.mx == INFINITY)
+  if (mx != mx)
+    *result = T(mx);  // NaN
+  else if (mx == INFINITY)
     *result = T(INFINITY);
   else
     *result = T(sqrt(g.ss));
@@ -310,10 +359,7 @@ __global__ void __launch_bounds__(kT) nrm2_rescaled_kernel(long n, const T *__re
   const T sc = T(ldexp(1.0, -e));  // exact power of two
   SumSq<T> acc[kU];
   for_each(n, x, inc, vec, [&](int u, T v, long) { acc[u].add(v * sc); });
-  double ss0 = 0.0;
-#pragma unroll
-  for (int u = 0; u < kU; ++u) ss0 += acc[u].get();
-  Part2 tot = part2_reduce_block(Part2{ss0, 0.0}, sh);
+  Part2 tot = sumsq_block<T>(acc, 0u, sh);
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = tot;
     __threadfence();
@@ -322,9 +368,9 @@ __global__ void __launch_bounds__(kT) nrm2_rescaled_kernel(long n, const T *__re
   __syncthreads();
   if (!last) return;
   __threadfence();
-  Part2 mine{0.0, 0.0};
-  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) mine.ss += __ldcg(&partials[b].ss);
-  const double ss = part2_reduce_block(mine, sh).ss;
+  double part = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) part += __ldcg(&partials[b].ss);
+  const double ss = part2_block(part, 0u, sh).ss;
   if (threadIdx.x != 0) return;
   *counter = 0;
   *const_cast<int *>(flag) = 0;  // every CTA has read it; the word returns to zero

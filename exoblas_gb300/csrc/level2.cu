@@ -324,7 +324,7 @@ __device__ __forceinline__ void symv_tile(T (&av)[PASSES][VN], T (&xc)[VN], T (&
 }
 
 template <typename T, bool VEC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 4 : 2)
     symv_strip_kernel(long n, long nt, const T *__restrict__ A, long lda, const T *__restrict__ x, T *__restrict__ P,
                       bool upper) {
   constexpr int VN = V16<T>::N;
