@@ -10,11 +10,22 @@ namespace l2 {
 
 constexpr int kThreads = 256;
 
-// Contiguous copy of a strided vector (element i of src at src[i*inc]).
+// Contiguous copy of a strided vector (element i of src at src[i*inc]);
+// 16-byte vectors when the copy is unit-stride and both ends are aligned.
 template <typename T>
 __global__ void pack_kernel(long n, const T *__restrict__ src, long inc, T *__restrict__ dst) {
-  for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x)
-    dst[i] = src[i * inc];
+  const long stride = long(gridDim.x) * blockDim.x, t = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (inc == 1 && ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+    using V = typename V16<T>::type;
+    constexpr int VN = V16<T>::N;
+    const long nv = n / VN;
+    const V *s = reinterpret_cast<const V *>(src);
+    V *d = reinterpret_cast<V *>(dst);
+    for (long i = t; i < nv; i += stride) d[i] = ld_stream(s + i);
+    for (long i = nv * VN + t; i < n; i += stride) dst[i] = src[i];
+    return;
+  }
+  for (long i = t; i < n; i += stride) dst[i] = src[i * inc];
 }
 // ------------------------------------------------------------ row dots ----
 // out_i = sum_{j in [lo(i), hi(i))} A[i,j] * x[j] for every row i, G threads
