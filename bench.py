@@ -17,7 +17,10 @@ value      aggregate algorithmic GB/s (decimal) of the set, device-resident
            CUDA events on the library's stream.
 e2e        the same set through the same entry points with pinned HOST
            buffers: the library stages every operand host->device and copies
-           outputs back inside the timed region (wall clock).
+           outputs back inside the timed region (wall clock).  It also
+           carries this box's pinned copy rates and frac_of_link_bound: the
+           time the copies alone (at those rates) plus the device step take,
+           over the measured e2e step.
 roofline   the kernel with the largest share of the step, against the
            measured HBM copy bandwidth in MEASURED_PEAKS.json.
 cpu_baseline  the CPU oracle (C++ restatement of the reference algorithms,
@@ -298,6 +301,25 @@ def cpu_baseline(min_seconds=10.0):
             "sample": f"{SAMPLE_DESC}; {reps} passes, {total_t:.1f} s"}
 
 
+def host_link_rates(local, nbytes=1 << 30):
+    """Pinned host <-> device copy rates (GB/s) of this box, 1 GiB each way."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{local}")
+    out = []
+    for src, dst in ((h, d), (d, h)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        out.append(3 * nbytes / (time.perf_counter() - t0) / 1e9)
+    del h, d
+    return out[0], out[1]
+
+
 def openblas_step(S):
     """One pass of the CPU sample through SciPy's bundled OpenBLAS (the CBLAS
     the reference compares against); returns per-kernel seconds."""
@@ -479,9 +501,15 @@ def main():
             tt = torch.tensor([e2e_s], device=f"cuda:{local}")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             e2e_s = float(tt.item())
+        h2d_step, d2h_step = (h1.value - h0.value) // KE, (d1.value - d0.value) // KE
+        link_h, link_d = host_link_rates(local)
+        # time the host link alone would need per step (copies in, device
+        # work, copies out, one after another) over the measured step time
+        ideal = h2d_step / (link_h * 1e9) + d2h_step / (link_d * 1e9) + ms_per_step * 1e-3
         e2e = {"value": round(world * step_bytes * KE / e2e_s / 1e9, 2), "unit": UNIT,
-               "h2d_bytes_per_step": (h1.value - h0.value) // KE, "d2h_bytes_per_step": (d1.value - d0.value) // KE,
-               "steps": KE}
+               "h2d_bytes_per_step": h2d_step, "d2h_bytes_per_step": d2h_step, "steps": KE,
+               "link_h2d_gbs": round(link_h, 1), "link_d2h_gbs": round(link_d, 1),
+               "frac_of_link_bound": round(ideal / (e2e_s / KE), 3)}
 
     cpu = openblas = None
     if rank == 0 and not args.no_cpu_baseline:
