@@ -92,6 +92,7 @@ EXTRA = {
     "exoblas_get_stream": ("p", ""),
     "exoblas_set_blocking": ("i", "i"),
     "exoblas_synchronize": ("i", ""),
+    "exoblas_selftest_wait_timeout": ("i", "d"),
     "exoblas_set_precision": ("i", "i"),
     "exoblas_get_precision": ("i", ""),
     "exoblas_kernel_launches": ("u", ""),

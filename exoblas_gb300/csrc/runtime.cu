@@ -247,6 +247,26 @@ void report(int status, const char *fn, const char *msg) {
 
 using namespace exb;
 
+// A wait on a device flag that nothing sets, bounded by `limit_ns` of the
+// global timer; on expiry it records the timeout in the status word, as the
+// solvers' bounded waits do, and returns.
+__global__ void expiring_wait_kernel(const int *flag, unsigned long long limit_ns, int *status) {
+  if (threadIdx.x != 0) return;
+  unsigned long long t0, t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+    if (v != 0) return;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > limit_ns) {
+      atomicExch(status, 1);
+      return;
+    }
+    __nanosleep(1000);
+  }
+}
+
 extern "C" {
 
 int exoblas_get_status(void) { return tl_status; }
@@ -317,6 +337,22 @@ int exoblas_get_precision(void) {
   int p = EXOBLAS_PRECISION_NATIVE;
   guarded("exoblas_get_precision", [&] { p = ctx().precision; });
   return p;
+}
+
+int exoblas_selftest_wait_timeout(double seconds) {
+  return guarded("exoblas_selftest_wait_timeout", [&] {
+    if (!(seconds > 0.0 && seconds <= 1.0)) fail(EXOBLAS_INVALID_VALUE, "seconds must lie in (0, 1]");
+    Context &c = ctx();
+    int *flag = static_cast<int *>(scratch(256));
+    EXB_CUDA(cudaMemsetAsync(flag, 0, 4, c.stream));
+    expiring_wait_kernel<<<1, 32, 0, c.stream>>>(flag, static_cast<unsigned long long>(seconds * 1e9),
+                                                 device_status_word());
+    EXB_LAUNCH("expiring-wait kernel");
+    count_launch();
+    c.status_pending = true;
+    EXB_CUDA(cudaStreamSynchronize(c.stream));
+    check_device_status();  // the recorded expiry surfaces as EXOBLAS_TIMEOUT
+  });
 }
 
 unsigned long long exoblas_kernel_launches(void) { return g_launches.load(); }

@@ -84,6 +84,12 @@ EXOBLAS_API int exoblas_set_blocking(int blocking);
 /* Waits for the thread's queued work.  Also reports EXOBLAS_TIMEOUT when a
  * kernel queued in non-blocking mode (trsv) gave up a bounded wait. */
 EXOBLAS_API int exoblas_synchronize(void);
+/* Self-test of the bounded-wait path (no reference counterpart): launches one
+ * kernel that waits on a device flag nothing sets, gives up after `seconds`
+ * (0 < seconds <= 1), records the expiry in the device status word and
+ * returns.  The call then reports EXOBLAS_TIMEOUT through the same path as
+ * the solvers' bounded waits; the thread's context stays usable. */
+EXOBLAS_API int exoblas_selftest_wait_timeout(double seconds);
 
 /* Arithmetic used by exo_sgemm/ssymm/ssyrk/ssyr2k and exo_dgemm/dsymm/dsyrk/dsyr2k:
  *   EXOBLAS_PRECISION_NATIVE    FP32 FFMA / FP64 DFMA kernels (default)
