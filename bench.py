@@ -370,6 +370,18 @@ def openblas_baseline(seconds_each=5.0):
     return out
 
 
+# --------------------------------------------------------------- replicas --
+def max_over_ranks(dist, value, device):
+    """The largest `value` over all ranks (the replicas' slowest time).  The
+    bench's GPU ranks pass a CUDA device (NCCL); the same host logic runs
+    over gloo with device "cpu" in the multi-process CPU tests."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ------------------------------------------------------------------- main --
 def main():
     args = parse()
@@ -454,9 +466,7 @@ def main():
         raise RuntimeError("library reported a failure in the timed region")
     total_ms = t_start.elapsed_time(t_end)
     if dist:
-        tt = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+        total_ms = max_over_ranks(dist, total_ms, f"cuda:{local}")
         dist.barrier()
 
     per = {k: statistics.mean(evs[s][i][0].elapsed_time(evs[s][i][1]) for s in range(K)) for i, k in enumerate(names)}
@@ -498,9 +508,7 @@ def main():
             raise RuntimeError("library reported a failure in the e2e region")
         e2e_s = t1 - t0
         if dist:
-            tt = torch.tensor([e2e_s], device=f"cuda:{local}")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_s = float(tt.item())
+            e2e_s = max_over_ranks(dist, e2e_s, f"cuda:{local}")
         h2d_step, d2h_step = (h1.value - h0.value) // KE, (d1.value - d0.value) // KE
         link_h, link_d = host_link_rates(local)
         # time the host link alone would need per step (copies in, device
