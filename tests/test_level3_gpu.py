@@ -78,3 +78,43 @@ def test_sgemm_config_1024(cuda):
     ref = A.astype(np.float64) @ B.astype(np.float64) + 0.5 * C.astype(np.float64)
     mag = np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64)) + 0.5 * np.abs(C.astype(np.float64))
     assert np.all(np.abs(out - ref) <= 4 * n * EPS["s"] * mag)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_beta_zero_multiplies_c(cuda, mode):
+    """Level 3 scales C by beta as a multiplication even when beta == 0
+    (src/level3/mscal.py:12-28), so a NaN in C stays NaN; every precision
+    path (native, split-BF16, Ozaki) keeps that."""
+    import exoblas_gb300 as eb
+
+    g = np.random.default_rng(23)
+    m, n, k = 70, 66, 40
+    eb.set_precision(mode)
+    try:
+        for p, dt in (("s", np.float32), ("d", np.float64)):
+            A = g.uniform(-1, 1, (m, k)).astype(dt)
+            B = g.uniform(-1, 1, (k, n)).astype(dt)
+            C = g.uniform(-1, 1, (m, n)).astype(dt)
+            C[5, 9] = np.nan
+            getattr(eb, f"exo_{p}gemm")(101, 111, 111, m, n, k, 1.0, A, k, B, n, 0.0, C, n)
+            assert np.isnan(C[5, 9]) and np.isfinite(np.delete(C.ravel(), 5 * n + 9)).all()
+
+            S = g.uniform(-1, 1, (m, m)).astype(dt)
+            C = g.uniform(-1, 1, (m, n)).astype(dt)
+            C[7, 3] = np.nan
+            Bs = g.uniform(-1, 1, (m, n)).astype(dt)
+            getattr(eb, f"exo_{p}symm")(101, 141, 121, m, n, 1.0, S, m, Bs, n, 0.0, C, n)
+            assert np.isnan(C[7, 3]) and np.isfinite(np.delete(C.ravel(), 7 * n + 3)).all()
+
+            Ak = g.uniform(-1, 1, (m, k)).astype(dt)
+            C = g.uniform(-1, 1, (m, m)).astype(dt)
+            C[9, 2] = np.nan   # inside the lower triangle
+            C[1, 8] = np.nan   # outside it: left alone
+            getattr(eb, f"exo_{p}syrk")(101, 122, 111, m, k, 1.0, Ak, k, 0.0, C, m)
+            assert np.isnan(C[9, 2]) and np.isnan(C[1, 8])
+            mask = np.ones_like(C, dtype=bool)
+            mask[9, 2] = mask[1, 8] = False
+            assert np.isfinite(C[mask & np.tril(np.ones_like(mask))]).all()
+    finally:
+        eb.set_precision(0)
