@@ -83,3 +83,30 @@ def test_bandwidth_sizes_properties(cuda):
     xd, yd = x[:n].double(), y[:n].double()
     got = eb.exo_ddot(n, xd, 1, yd, 1)
     assert abs(got - torch.dot(xd, yd).item()) <= 4 * n * np.finfo(np.float64).eps * torch.dot(xd.abs(), yd.abs()).item()
+
+
+@pytest.mark.gpu
+def test_int_max_length_vectors(cuda):
+    """N = 2^31 - 1, the largest the int-typed CBLAS signatures carry, on
+    device operands (8 GiB each): exact size-independent properties, so
+    every element and every index path (32-bit loop indices included) is
+    exercised without a CPU oracle of that size."""
+    import torch
+
+    import exoblas_gb300 as eb
+
+    n = 2**31 - 1
+    x = torch.ones(n, dtype=torch.float32, device="cuda")
+    y = torch.full((n,), 2.0, dtype=torch.float32, device="cuda")
+    eb.exo_saxpy(n, 3.0, x, 1, y, 1)  # every y becomes 5 exactly
+    torch.cuda.synchronize()
+    assert bool((y == 5.0).all())
+    assert float(y[-1]) == 5.0 and float(y[0]) == 5.0
+    # asum of 5s: partial sums stay exact in FP32 up to 2^24, the total rounds once
+    r = eb.exo_sasum(n, y, 1)
+    assert abs(r - 5.0 * n) <= 5.0 * n * 2**-20
+    # i?amax: the single largest element sits at the last index
+    y[-1] = 7.0
+    assert eb.exo_isamax(n, y, 1) == n - 1
+    del x, y
+    torch.cuda.empty_cache()
