@@ -123,3 +123,30 @@ def test_trsv_clustered_sizes(cuda, case):
     o_r, o_a = run_oracle(case)
     assert_rel1pct(a[7], o_a[7], f"{case}")
     trsv_residual_ok(case, a[7])
+
+
+@pytest.mark.gpu
+def test_matrices_past_int32_elements(cuda):
+    """n = 46341, so n * n > 2^31 elements (8.6 GB of FP32): gemv N / T and
+    symv with A = ones and x = ones give y = n exactly (integer partial sums
+    below 2^24 are exact in FP32), which exercises every row and column and
+    the 64-bit element offsets."""
+    import torch
+
+    import exoblas_gb300 as eb
+
+    n = 46341
+    A = torch.ones((n, n), dtype=torch.float32, device="cuda")
+    x = torch.ones(n, dtype=torch.float32, device="cuda")
+    for trans in (111, 112):
+        y = torch.zeros(n, dtype=torch.float32, device="cuda")
+        eb.exo_sgemv(101, trans, n, n, 1.0, A, n, x, 1, 0.0, y, 1)
+        torch.cuda.synchronize()
+        assert bool((y == float(n)).all()), trans
+    for uplo in (121, 122):
+        y = torch.zeros(n, dtype=torch.float32, device="cuda")
+        eb.exo_ssymv(101, uplo, n, 1.0, A, n, x, 1, 0.0, y, 1)
+        torch.cuda.synchronize()
+        assert bool((y == float(n)).all()), uplo
+    del A, x, y
+    torch.cuda.empty_cache()
