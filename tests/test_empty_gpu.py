@@ -61,3 +61,23 @@ def test_empty_cases_run_on_the_oracle():
 def test_empty_and_degenerate_sizes(cuda, case):
     r, a = run_gpu(case)
     check_case(case, r, a)
+
+
+EMPTY_L3 = [c for c in EMPTY if c.op[1:] in ("gemm", "symm", "syrk", "syr2k")]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [1, 2], ids=["split_bf16", "ozaki"])
+def test_degenerate_level3_on_precision_paths(cuda, mode):
+    """The same degenerate level-3 shapes on the split-BF16 (FP32) and Ozaki
+    (FP64) paths: K = 0 takes the native kernels, and 1 x 1 or 3 x 3 outputs
+    ride the tensor-core kernels with padded tiles."""
+    import exoblas_gb300 as eb
+
+    eb.set_precision(mode)
+    try:
+        for case in EMPTY_L3:
+            r, a = run_gpu(case)
+            check_case(case, r, a)
+    finally:
+        eb.set_precision(0)
