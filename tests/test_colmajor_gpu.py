@@ -211,3 +211,50 @@ def test_colmajor_rejected_by_default(cuda):
     C = np.zeros(4, np.float32)
     with pytest.raises(eb.UnsupportedParameterException):
         eb.exo_sgemm(COL, NT, NT, 2, 2, 2, 1.0, C, 2, C, 2, 0.0, C.copy(), 2)
+
+
+def band_cm(buf, n, k, lda, upper):
+    """Dense n x n matrix from CBLAS column-major band storage: column j holds
+    rows max(0, j-k)..j at buf[j*lda + k + i - j] (upper) or rows
+    j..min(n-1, j+k) at buf[j*lda + i - j] (lower)."""
+    A = np.zeros((n, n))
+    for j in range(n):
+        rows = range(max(0, j - k), j + 1) if upper else range(j, min(n, j + k + 1))
+        for i in rows:
+            A[i, j] = buf[j * lda + (k + i - j if upper else i - j)]
+    return A
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("p", "sd")
+@pytest.mark.parametrize("u", [UP, LO])
+def test_band_colmajor(colmajor, p, u):
+    eb, g = colmajor, np.random.default_rng(6)
+    n, k = 90, 7
+    lda = k + 3
+    a = (g.uniform(-1, 1, lda * n) / 100).astype(DT[p])
+    for j in range(n):  # diagonal entries 2, as the reference's tbsv test
+        a[j * lda + (k if u == UP else 0)] = 2
+    B = band_cm(a.astype(np.float64), n, k, lda, u == UP)
+    x = g.uniform(-1, 1, n).astype(DT[p])
+    y = g.uniform(-1, 1, n).astype(DT[p])
+    x64, y64 = x.astype(np.float64), y.astype(np.float64)
+    # sbmv: the stored triangle defines the symmetric band matrix
+    S = B + B.T - np.diag(np.diag(B))
+    yy = y.copy()
+    getattr(eb, f"exo_{p}sbmv")(COL, u, n, k, 1.3, a, lda, x, 1, 0.4, yy, 1)
+    check(yy, 1.3 * S @ x64 + 0.4 * y64, 1.3 * np.abs(S) @ np.abs(x64) + 0.4 * np.abs(y64), 2 * k + 2, p, "sbmv")
+    for t in (NT, TR):
+        for d in (NU, UN):
+            T = B.copy()
+            if d == UN:
+                np.fill_diagonal(T, 1.0)
+            opT = T if t == NT else T.T
+            xm = x.copy()
+            getattr(eb, f"exo_{p}tbmv")(COL, u, t, d, n, k, a, lda, xm, 1)
+            check(xm, opT @ x64, np.abs(opT) @ np.abs(x64), k + 2, p, f"tbmv t={t} d={d}")
+            b = x.copy()
+            getattr(eb, f"exo_{p}tbsv")(COL, u, t, d, n, k, a, lda, b, 1)
+            b64 = b.astype(np.float64)
+            r = opT @ b64 - x64
+            check(r, 0 * r, np.abs(opT) @ np.abs(b64), 2 * (k + 1), p, f"tbsv residual t={t} d={d}")
