@@ -121,6 +121,15 @@ SIGS = {
     "oracle_par_sgemm": ("v", "iiiiiifpipifpi"),
 }
 
+# Double-word (about 104-bit) instantiations of the restatements: same
+# arguments as the d-variant, every array a {hi, lo} pair array.
+DW_OPS = (
+    "dasum daxpy ddot dscal drot drotm dgemv dger dsymv dsyr dsyr2 dtrmv dtrsv dgemm dsymm dsyrk "
+    "dgbmv dsbmv dtbmv dtbsv dsyr2k dtrmm dnrm2"
+).split()
+for _op in DW_OPS:
+    SIGS["oracle_dw_" + _op] = SIGS["oracle_" + _op]
+
 _lib = None
 
 
@@ -154,3 +163,34 @@ def call(name: str, *args):
 
 def last_status() -> int:
     return lib().oracle_last_status()
+
+
+def call_dw(name: str, *args):
+    """Run the double-word instantiation oracle_dw_<name> (name a d-op such as
+    "dgemv") on float64 arguments.  Returns (result, args) like a plain call,
+    with every array argument replaced by a float64 copy holding the
+    double-word result rounded to double; the caller's arrays are untouched."""
+    import numpy as np
+
+    res, codes = SIGS["oracle_dw_" + name]
+    pairs, conv = [], []
+    for v, c in zip(args, codes):
+        if c == "p" and v is not None and not isinstance(v, int):
+            a = np.asarray(v, np.float64)
+            w = np.zeros(a.shape + (2,), np.float64)
+            w[..., 0] = a
+            pairs.append(w)
+            conv.append(w.ctypes.data)
+        else:
+            pairs.append(None)
+            conv.append(v)
+    r = getattr(lib(), "oracle_dw_" + name)(*conv)
+    out = []
+    for v, w in zip(args, pairs):
+        if w is None:
+            out.append(v)
+        else:
+            hi, lo = w[..., 0], w[..., 1]
+            with np.errstate(invalid="ignore", over="ignore"):
+                out.append(np.where(np.isfinite(hi), hi + lo, hi))
+    return r, out

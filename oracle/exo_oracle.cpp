@@ -921,6 +921,76 @@ inline DD dd_norm(DD v) {
   return DD{s, e};
 }
 
+// ------------------------------------------- double-word arithmetic type --
+// Dw is a number type with about 104 significand bits, so the restatements
+// above can be instantiated with T = Dw and give the same loop nest evaluated
+// in double-word arithmetic: the high-precision reference for d-precision
+// results.  Algorithms from Joldes, Muller and Popescu, "Tight and rigorous
+// error bounds for basic building blocks of double-word arithmetic", ACM TOMS
+// 44(2), 2017: sum of two double-words (their Algorithm 6, relative error
+// below 3u^2), product (Algorithm 12, below 5u^2) and a quotient by one
+// correction step of the high-part quotient (below 2^-100 relative).  Inputs
+// enter as {x, 0}, so every input is exact.  A non-finite high part wins
+// over the low part when results are read back (Dw::value()).
+
+inline void fast_two_sum(double a, double b, double &s, double &e) {
+  s = a + b;
+  e = b - (s - a);
+}
+
+struct Dw {
+  double hi = 0.0, lo = 0.0;
+  Dw() = default;
+  Dw(double v) : hi(v), lo(0.0) {}  // NOLINT: implicit, like a double literal
+  Dw(double h, double l) : hi(h), lo(l) {}
+  double value() const { return std::isfinite(hi) ? hi + lo : hi; }
+};
+static_assert(sizeof(Dw) == 2 * sizeof(double), "Dw is two packed doubles");
+
+inline Dw operator+(Dw x, Dw y) {
+  if (!std::isfinite(x.hi) || !std::isfinite(y.hi)) return Dw(x.hi + y.hi);
+  double sh, sl, th, tl, vh, vl, zh, zl;
+  two_sum(x.hi, y.hi, sh, sl);
+  two_sum(x.lo, y.lo, th, tl);
+  const double c = sl + th;
+  fast_two_sum(sh, c, vh, vl);
+  const double w = tl + vl;
+  fast_two_sum(vh, w, zh, zl);
+  return Dw(zh, zl);
+}
+inline Dw operator-(Dw x) { return Dw(-x.hi, -x.lo); }
+inline Dw operator-(Dw x, Dw y) { return x + (-y); }
+inline Dw operator*(Dw x, Dw y) {
+  double ch, cl1;
+  two_prod(x.hi, y.hi, ch, cl1);
+  if (!std::isfinite(ch) || ch == 0.0) return Dw(ch);
+  const double tl0 = x.lo * y.lo;
+  const double tl1 = std::fma(x.hi, y.lo, tl0);
+  const double cl2 = std::fma(x.lo, y.hi, tl1);
+  const double cl3 = cl1 + cl2;
+  double zh, zl;
+  fast_two_sum(ch, cl3, zh, zl);
+  return Dw(zh, zl);
+}
+inline Dw operator/(Dw x, Dw y) {
+  const double q1 = x.hi / y.hi;
+  if (!std::isfinite(q1) || q1 == 0.0) return Dw(q1);
+  const Dw r = x - y * Dw(q1);
+  const double q2 = r.hi / y.hi;
+  const Dw r2 = r - y * Dw(q2);
+  const double q3 = r2.hi / y.hi;
+  double s, e;
+  fast_two_sum(q1, q2, s, e);
+  return Dw(s, e) + Dw(q3);
+}
+inline Dw &operator+=(Dw &x, Dw y) { return x = x + y; }
+inline Dw &operator-=(Dw &x, Dw y) { return x = x - y; }
+inline Dw &operator*=(Dw &x, Dw y) { return x = x * y; }
+inline bool operator==(Dw x, Dw y) { return x.hi == y.hi && x.lo == y.lo; }
+inline bool operator!=(Dw x, Dw y) { return !(x == y); }
+inline bool operator<(Dw x, Dw y) { return x.hi < y.hi || (x.hi == y.hi && x.lo < y.lo); }
+inline bool operator>(Dw x, Dw y) { return y < x; }
+
 // ------------------------------------------------------ threaded drivers --
 
 template <typename F>
@@ -1054,6 +1124,65 @@ ORACLE_API void oracle_ssyr2k(int order, int Uplo, int Trans, int N, int K, floa
 ORACLE_API void oracle_dsyr2k(int order, int Uplo, int Trans, int N, int K, double alpha, const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc) { syr2k_wrap<double>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
 ORACLE_API void oracle_strmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, float alpha, const float *A, int lda, float *B, int ldb) { trmm_wrap<float>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }
 ORACLE_API void oracle_dtrmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, double alpha, const double *A, int lda, double *B, int ldb) { trmm_wrap<double>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }
+
+// ----- the same restatements in double-word arithmetic (T = Dw)
+// Arguments as oracle_d<op>; every array is a Dw array (pairs {hi, lo} of
+// doubles, inputs entered as {x, 0}), scalars are doubles, and returned
+// scalars are rounded to double.  These are the d-precision references.
+
+ORACLE_API double oracle_dw_dasum(int N, const Dw *X, int incX) { return asum_wrap<Dw>(N, X, incX).value(); }
+ORACLE_API void oracle_dw_daxpy(int N, double alpha, const Dw *X, int incX, Dw *Y, int incY) { axpy_wrap<Dw>(N, alpha, X, incX, Y, incY); }
+ORACLE_API double oracle_dw_ddot(int N, const Dw *X, int incX, const Dw *Y, int incY) { return dot_wrap<Dw>(N, X, incX, Y, incY).value(); }
+ORACLE_API void oracle_dw_dscal(int N, double alpha, Dw *X, int incX) { scal_wrap<Dw>(N, alpha, X, incX); }
+ORACLE_API void oracle_dw_drot(int N, Dw *X, int incX, Dw *Y, int incY, double c, double s) {
+  two_vec_wrap_prep<Dw>(N, X, incX, Y, incY);
+  rot_proc<Dw>(N, Vec<Dw>{X, incX}, Vec<Dw>{Y, incY}, c, s);
+}
+ORACLE_API void oracle_dw_drotm(int N, Dw *X, int incX, Dw *Y, int incY, const Dw *P) {
+  two_vec_wrap_prep<Dw>(N, X, incX, Y, incY);
+  rotm_proc<Dw>(N, Vec<Dw>{X, incX}, Vec<Dw>{Y, incY}, P);
+}
+ORACLE_API void oracle_dw_dgemv(int order, int TransA, int M, int N, double alpha, const Dw *A, int lda, const Dw *X, int incX, double beta, Dw *Y, int incY) { gemv_wrap<Dw>(order, TransA, M, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dw_dger(int order, int M, int N, double alpha, const Dw *X, int incX, const Dw *Y, int incY, Dw *A, int lda) { ger_wrap<Dw>(order, M, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_dw_dsymv(int order, int Uplo, int N, double alpha, const Dw *A, int lda, const Dw *X, int incX, double beta, Dw *Y, int incY) { symv_wrap<Dw>(order, Uplo, N, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dw_dsyr(int order, int Uplo, int N, double alpha, const Dw *X, int incX, Dw *A, int lda) { syr_wrap<Dw>(order, Uplo, N, alpha, X, incX, A, lda); }
+ORACLE_API void oracle_dw_dsyr2(int order, int Uplo, int N, double alpha, const Dw *X, int incX, const Dw *Y, int incY, Dw *A, int lda) { syr2_wrap<Dw>(order, Uplo, N, alpha, X, incX, Y, incY, A, lda); }
+ORACLE_API void oracle_dw_dtrmv(int order, int Uplo, int TransA, int Diag, int N, const Dw *A, int lda, Dw *X, int incX) { trmv_wrap<Dw>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+ORACLE_API void oracle_dw_dtrsv(int order, int Uplo, int TransA, int Diag, int N, const Dw *A, int lda, Dw *X, int incX) { trsv_wrap<Dw>(order, Uplo, TransA, Diag, N, A, lda, X, incX); }
+ORACLE_API void oracle_dw_dgemm(int order, int TransA, int TransB, int M, int N, int K, double alpha, const Dw *A, int lda, const Dw *B, int ldb, double beta, Dw *C, int ldc) { gemm_wrap<Dw>(order, TransA, TransB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dw_dsymm(int order, int Side, int Uplo, int M, int N, double alpha, const Dw *A, int lda, const Dw *B, int ldb, double beta, Dw *C, int ldc) { symm_wrap<Dw>(order, Side, Uplo, M, N, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dw_dsyrk(int order, int Uplo, int Trans, int N, int K, double alpha, const Dw *A, int lda, double beta, Dw *C, int ldc) { syrk_wrap<Dw>(order, Uplo, Trans, N, K, alpha, A, lda, beta, C, ldc); }
+ORACLE_API void oracle_dw_dgbmv(int M, int N, int KL, int KU, double alpha, const Dw *A, int lda, const Dw *X, int incX, double beta, Dw *Y, int incY) { gbmv_wrap<Dw>(M, N, KL, KU, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dw_dsbmv(int order, int Uplo, int N, int K, double alpha, const Dw *A, int lda, const Dw *X, int incX, double beta, Dw *Y, int incY) { sbmv_wrap<Dw>(order, Uplo, N, K, alpha, A, lda, X, incX, beta, Y, incY); }
+ORACLE_API void oracle_dw_dtbmv(int order, int Uplo, int TransA, int Diag, int N, int K, const Dw *A, int lda, Dw *X, int incX) { tb_wrap<Dw>(false, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
+ORACLE_API void oracle_dw_dtbsv(int order, int Uplo, int TransA, int Diag, int N, int K, const Dw *A, int lda, Dw *X, int incX) { tb_wrap<Dw>(true, order, Uplo, TransA, Diag, N, K, A, lda, X, incX); }
+ORACLE_API void oracle_dw_dsyr2k(int order, int Uplo, int Trans, int N, int K, double alpha, const Dw *A, int lda, const Dw *B, int ldb, double beta, Dw *C, int ldc) { syr2k_wrap<Dw>(order, Uplo, Trans, N, K, alpha, A, lda, B, ldb, beta, C, ldc); }
+ORACLE_API void oracle_dw_dtrmm(int order, int Side, int Uplo, int TransA, int Diag, int M, int N, double alpha, const Dw *A, int lda, Dw *B, int ldb) { trmm_wrap<Dw>(order, Side, Uplo, TransA, Diag, M, N, alpha, A, lda, B, ldb); }
+
+// nrm2 with the same scaling as nrm2_ref, the sum of squares in double-word
+// and a double-word square root (one Newton correction of sqrt(hi)).
+ORACLE_API double oracle_dw_dnrm2(int N, const Dw *X, int incX) {
+  g_status = 0;
+  if (N < 1) return 0.0;
+  if (incX < 0) X = X + long(1 - N) * incX;
+  double scale = 0;
+  bool nan = false;
+  for (long i = 0; i < N; ++i) {
+    const double v = std::fabs(X[i * incX].hi);
+    if (v != v) nan = true;
+    if (v > scale) scale = v;
+  }
+  if (nan) return NAN;
+  if (scale == 0 || std::isinf(scale)) return scale;
+  Dw ss(0.0);
+  for (long i = 0; i < N; ++i) {
+    const Dw v = X[i * incX] / Dw(scale);
+    ss += v * v;
+  }
+  const double s0 = std::sqrt(ss.hi);
+  const Dw root = Dw(s0) + (ss - Dw(s0) * Dw(s0)) / Dw(2.0 * s0);
+  return (Dw(scale) * root).value();
+}
 
 // ----- double-double high-precision references (results rounded to double)
 

@@ -13,7 +13,8 @@ define them:
   every output buffer, padding included (test/common/correctness_helpers.h:
   9-16, generate_buffer.h:57-68);
 - the componentwise bound |r - e| <= c * n * eps * m, where e is an FP64
-  result, n the reduction length and m the same operation evaluated on
+  result for s-precision and a double-word (about 104-bit) result for
+  d-precision, n the reduction length and m the same operation evaluated on
   absolute values (|alpha||A||x| + |beta||y| for gemv, and so on);
 - bit-exactness for copy, swap and scal by +-1.
 """
@@ -195,10 +196,28 @@ def _magnitude(c64: Case):
     return run_oracle(magnitude_case(c64))
 
 
+def run_dw(case64: Case):
+    """The oracle's double-word instantiation of a d-op (about 104 significand
+    bits), rounded to double; None when the op has none (exact ops, iamax)."""
+    import oracle
+
+    if case64.op not in oracle.DW_OPS:
+        return None
+    return oracle.call_dw(case64.op, *case64.clone_args())
+
+
 def fp64_reference(case: Case):
-    """FP64 result and magnitude for a case (via the oracle's d-variant)."""
+    """High-precision result and FP64 magnitude for a case.
+
+    s-precision (and sdsdot): the oracle's d-variant in FP64, whose own
+    rounding is far below the FP32 bound.  d-precision (and dsdot): the same
+    restated loop nest in double-word arithmetic, so the FP64 result under
+    test is measured against a reference that does not carry FP64 rounding.
+    The magnitude (the op on absolute values) is an FP64 run either way; it
+    only scales the bound."""
     c64 = to64(case)
-    r64, a64 = run_oracle(c64)
+    hp = run_dw(c64) if case.p == "d" else None
+    r64, a64 = hp if hp is not None else run_oracle(c64)
     m, am = _magnitude(c64)
     if case.op == "sdsdot":
         r64 = r64 + case.args[1]
@@ -222,3 +241,54 @@ def check_case(case: Case, got_r, got_args, c=4.0, what="gpu"):
     for i in case.outputs:
         assert_rel1pct(got_args[i], o_args[i], f"{what} {case} out{i}")
         assert_bound(got_args[i], a64[i], am[i], case.nred, p, c, f"{what} {case} out{i}")
+
+
+def _tr_product(op, args, xs, d_prec):
+    """op(A) xs for a triangular (dtrmv) or banded triangular (dtbmv) matrix:
+    double-word for d-precision, so the residual carries no FP64 rounding of
+    its own; FP64 for s-precision."""
+    import oracle
+
+    if d_prec:
+        _, out = oracle.call_dw(op, *args[:-2], xs, args[-1])
+        return out[-2]
+    r = xs.copy()
+    oracle.call(op, *args[:-2], r, args[-1])
+    return r
+
+
+def trsv_residual_ok(case: Case, xhat: np.ndarray, c=8.0):
+    """|b - op(A) xhat| <= c n eps |op(A)| |xhat| componentwise.  The product
+    op(A) xhat is formed in double-word for dtrsv and FP64 for strsv."""
+    import oracle
+
+    order, u, t, d, n, A, lda, x, inc = case.args
+    step = abs(inc)
+    b = x.astype(np.float64)[::step][:n]
+    xs = xhat.astype(np.float64)[::step][:n]
+    if inc < 0:
+        b, xs = b[::-1].copy(), xs[::-1].copy()
+    A64 = A.astype(np.float64)
+    r = _tr_product("dtrmv", [order, u, t, d, n, A64, lda, None, 1], xs, case.p == "d")
+    m = np.abs(xs)
+    oracle.call("dtrmv", order, u, t, d, n, np.abs(A64), lda, m, 1)
+    eps = EPS[case.p]
+    bad = np.abs(b - r) > c * max(n, 1) * eps * m + 1e-300
+    assert not bad.any(), f"{case}: residual bound fails at {np.flatnonzero(bad)[:5]}"
+
+
+def tbsv_residual_ok(case: Case, xhat: np.ndarray, c=8.0):
+    """|b - op(A) xhat| <= c (k + 1) eps |op(A)| |xhat| componentwise, the
+    product in double-word for dtbsv and FP64 for stbsv."""
+    import oracle
+
+    order, u, t, d, n, k, A, lda, x, inc = case.args
+    A64 = A.astype(np.float64)
+    xs = xhat.astype(np.float64).copy()
+    r = _tr_product("dtbmv", [order, u, t, d, n, k, A64, lda, None, inc], xs, case.p == "d")
+    m = np.abs(xhat.astype(np.float64))
+    oracle.call("dtbmv", order, u, t, d, n, k, np.abs(A64), lda, m, inc)
+    b = x.astype(np.float64)
+    sel = np.arange(0, 1 + (n - 1) * abs(inc), abs(inc))
+    bad = np.abs(b[sel] - r[sel]) > c * (k + 1) * EPS[case.p] * m[sel] + 1e-300
+    assert not bad.any(), f"{case}: residual bound fails at {np.flatnonzero(bad)[:5]}"

@@ -1,10 +1,13 @@
 """Batched persistent execution: every instance of a mixed batch must match
-the CPU oracle for the same call (1% rule and componentwise FP bound), alone
-and inside the batch, for plain runs and CUDA-graph replays."""
+the CPU oracle for the same call (1% rule and componentwise FP bound; strsv by
+the residual bound), alone and inside the batch, for plain runs and
+CUDA-graph replays, including the full 4096-instance batch (m, n, k
+log-uniform in [16, 2048], seed 7)."""
 import numpy as np
 import pytest
 
-from common import EPS, LO, NT, NU, ROW, TR, UN, UP, Case, assert_bound, assert_rel1pct, fp64_reference, run_oracle
+from common import (EPS, LO, NT, NU, ROW, TR, UN, UP, Case, assert_bound, assert_rel1pct, fp64_reference, run_oracle,
+                    trsv_residual_ok)
 
 
 def _mixed_cases(seed=3, count=60):
@@ -63,6 +66,7 @@ def _check(case, got):
     j = case.outputs[0]
     assert_rel1pct(got, o_a[j], f"batch {case.op}")
     if case.op == "strsv":
+        trsv_residual_ok(case, got)
         return
     (r64, a64), (m, am) = fp64_reference(case)
     assert_bound(got, a64[j], am[j], case.nred, case.p, 4.0, f"batch {case.op}")
@@ -117,3 +121,60 @@ def test_autotuner_picks_valid_configs(cuda, tmp_path, monkeypatch):
     monkeypatch.setenv("EXOBLAS_TUNE_CACHE", str(tmp_path / "tune.json"))
     for m, n, k in [(16, 16, 16), (300, 200, 100), (2048, 2048, 2048)]:
         assert bt.tile_config(m, n, k) in (0, 1, 2)
+
+
+@pytest.mark.gpu
+def test_full_batch_every_instance(cuda):
+    """The 4096-instance batch of the benchmark (sgemm NN / dgemv N / strsv
+    lower no-trans non-unit, m, n, k log-uniform in [16, 2048], seed 7) run as
+    one plan: every sgemm against an FP64 product on the device within
+    4 (k + 1) eps_s |A||B| + ..., every dgemv against the oracle's
+    double-word gemv within 4 (n + 1) eps_d |A||x| + ..., every strsv by the
+    residual bound 8 n eps_s |L||x|.  The CUDA-graph replay of the same plan
+    from the same inputs must then give every output bit for bit."""
+    import oracle
+    from exoblas_gb300 import workloads
+    from exoblas_gb300.batch import BatchPlan
+
+    torch = cuda
+    ops, shapes, arena, views = workloads.batch_config(torch, "cuda")
+    assert len(views) == 4096
+    outs = [t[-1] for (_, _, t) in views]  # C, y, x: updated in place
+    start = [o.clone() for o in outs]
+    torch.cuda.synchronize()
+    plan = BatchPlan(ops)
+    plan.run()
+    torch.cuda.synchronize()
+    ran = [o.clone() for o in outs]
+    counts = {"sgemm": 0, "dgemv": 0, "strsv": 0}
+    for i, ((op, dims, t), c0) in enumerate(zip(views, start)):
+        counts[op] += 1
+        if op == "sgemm":
+            m, n, k = dims
+            A, B = t[0].view(m, k).double(), t[1].view(k, n).double()
+            C0 = c0.view(m, n).double()
+            ref = A @ B + 0.5 * C0
+            mag = A.abs() @ B.abs() + 0.5 * C0.abs()
+            err = (t[2].view(m, n).double() - ref).abs()
+            tol = 4.0 * (k + 1) * EPS["s"] * mag
+            assert bool((err <= tol).all()), f"sgemm instance {i} {dims}: max err/tol {float((err / tol).max())}"
+        elif op == "dgemv":
+            m, n = dims
+            A, x = t[0].cpu().numpy(), t[1].cpu().numpy()
+            y0 = c0.cpu().numpy()
+            _, hp = oracle.call_dw("dgemv", ROW, NT, m, n, 1.0, A, n, x, 1, 0.5, y0, 1)
+            mag = np.abs(A.reshape(m, n)) @ np.abs(x) + 0.5 * np.abs(y0)
+            assert_bound(t[2].cpu().numpy(), hp[10], mag, n + 1, "d", 4.0, f"dgemv instance {i} {dims}")
+        else:
+            (n,) = dims
+            case = Case("strsv", [ROW, LO, NT, NU, n, t[0].cpu().numpy(), n, c0.cpu().numpy(), 1], [7], nred=n + 1)
+            trsv_residual_ok(case, t[1].cpu().numpy())
+    assert min(counts.values()) > 1200, counts
+    for o, s0 in zip(outs, start):
+        o.copy_(s0)
+    torch.cuda.synchronize()
+    plan.graph_launch()
+    torch.cuda.synchronize()
+    for i, (o, r) in enumerate(zip(outs, ran)):
+        assert torch.equal(o, r), f"instance {i}: graph replay differs from the plan run"
+    plan.close()

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 from cases import gemv_cases, ger_cases, symv_cases, syr2_cases, syr_cases, trmv_cases, trsv_cases
-from common import EPS, Case, assert_rel1pct, check_case, run_gpu, run_oracle
+from common import EPS, assert_rel1pct, check_case, run_gpu, run_oracle, trsv_residual_ok
 
 GENERAL = (
     [c for p in "sd" for c in gemv_cases(p)]
@@ -27,26 +27,6 @@ def test_level2_host_pointers(cuda, case):
 def test_level2_device_pointers(cuda, case):
     r, a = run_gpu(case, device=True)
     check_case(case, r, a)
-
-
-def trsv_residual_ok(case: Case, xhat: np.ndarray, c=8.0):
-    """|b - op(A) xhat| <= c n eps |op(A)| |xhat| componentwise (FP64 residual)."""
-    import oracle
-
-    order, u, t, d, n, A, lda, x, inc = case.args
-    step = abs(inc)
-    b = x.astype(np.float64)[::step][:n]
-    xs = xhat.astype(np.float64)[::step][:n]
-    if inc < 0:
-        b, xs = b[::-1].copy(), xs[::-1].copy()
-    A64 = A.astype(np.float64)
-    r = xs.copy()
-    oracle.call("dtrmv", order, u, t, d, n, A64, lda, r, 1)
-    m = np.abs(xs)
-    oracle.call("dtrmv", order, u, t, d, n, np.abs(A64), lda, m, 1)
-    eps = EPS[case.p]
-    bad = np.abs(b - r) > c * n * eps * m + 1e-300
-    assert not bad.any(), f"{case}: residual bound fails at {np.flatnonzero(bad)[:5]}"
 
 
 TRSV = [c for p in "sd" for c in trsv_cases(p)] + [c for p in "sd" for c in trsv_cases(p, fixture=True)]

@@ -6,12 +6,16 @@
 2. The reference's deterministic trsv fixture (A = 2.0, X[i] = i).
 3. The wrapper special cases the oracle restates.
 4. A planted mistake in the oracle is caught by the same checks.
+5. The double-word instantiation (the d-precision reference): exact to the
+   last bit on small cases checked in rational arithmetic, within the bound
+   of every d-precision golden fixture, and the FP64 oracle within the bound
+   of it.
 """
 import numpy as np
 import pytest
 
 import golden_io
-from common import EPS, assert_bound, assert_rel1pct, fp64_reference, run_oracle
+from common import assert_bound, assert_rel1pct, fp64_reference, run_dw, run_oracle, to64
 
 FIXTURES = [(name, i) for name in golden_io.names() for i in range(len(golden_io.load(name)))]
 _cache = {}
@@ -111,3 +115,75 @@ def test_double_double_dot_is_exact_on_cancellation():
     x = np.array([1e16, 1.0, -1e16, 1.0])
     y = np.ones(4)
     assert oracle.call("dd_dot", 4, x, 1, y, 1) == 2.0
+
+
+D_FIXTURES = [(n, i) for n, i in FIXTURES if fixture(n, i)[0].p == "d" and not fixture(n, i)[0].exact]
+
+
+@pytest.mark.parametrize("name,i", D_FIXTURES, ids=lambda v: str(v))
+def test_double_word_reference_pins(name, i):
+    """Every d-precision fixture: the double-word restatement meets CBLAS's
+    outputs (1% rule, componentwise bound), and the plain FP64 oracle meets
+    the double-word result within the bound."""
+    case, exp_r, exp_out = fixture(name, i)
+    hp = run_dw(to64(case))
+    if hp is None:
+        pytest.skip(f"{case.op}: no double-word variant (exact or index result)")
+    (r, a), (m, am) = hp, fp64_reference(case)[1]
+    o_r, o_a = run_oracle(case)
+    tri_solve = case.op.endswith("trsv") or case.op.endswith("tbsv")
+    if case.scalar:
+        assert_rel1pct([r], [exp_r], f"dw {case}")
+        # OpenBLAS's dsdot accumulates in FP32 on this host: the FP32 bound
+        pcb = "s" if case.op == "dsdot" else "d"
+        assert_bound([exp_r], [r], [m], case.nred, pcb, 8.0, f"cblas {case} vs dw")
+        assert_bound([o_r], [r], [m], case.nred, "d", 8.0, f"oracle {case} vs dw")
+    for j, e in exp_out.items():
+        assert_rel1pct(a[j], e, f"dw {case} out{j}")
+        if not tri_solve:  # a solve's forward error is not held to a product bound
+            assert_bound(e, a[j], am[j], case.nred, "d", 8.0, f"cblas {case} out{j} vs dw")
+            assert_bound(o_a[j], a[j], am[j], case.nred, "d", 8.0, f"oracle {case} out{j} vs dw")
+
+
+def test_double_word_is_correctly_rounded_on_small_cases():
+    """dgemv, ddot and dtrsv (a unit lower matrix with integer entries, whose
+    solution is exact in rationals) in double-word arithmetic against exact
+    rational arithmetic: the rounded result is within half an ulp."""
+    from fractions import Fraction as F
+
+    import oracle
+
+    g = np.random.default_rng(5)
+    A = g.uniform(-1, 1, (23, 31))
+    x = g.uniform(-1, 1, 31)
+    y = g.uniform(-1, 1, 23)
+    _, out = oracle.call_dw("dgemv", 101, 111, 23, 31, 0.7, A, 31, x, 1, -0.3, y, 1)
+    for i in range(23):
+        ex = F(-0.3) * F(y[i]) + sum(F(0.7) * (F(x[j]) * F(A[i, j])) for j in range(31))
+        assert abs(F(out[10][i]) - ex) <= F(np.spacing(abs(float(ex)))) / 2
+    r, _ = oracle.call_dw("ddot", 31, x, 1, x[::-1].copy(), 1)
+    ex = sum(F(a) * F(b) for a, b in zip(x, x[::-1]))
+    assert abs(F(r) - ex) <= F(np.spacing(abs(float(ex)))) / 2
+    n = 12
+    L = np.tril(g.integers(-3, 4, (n, n)).astype(np.float64), -1) + np.eye(n)
+    b = g.uniform(-1, 1, n)
+    _, out = oracle.call_dw("dtrsv", 101, 122, 111, 132, n, L, n, b, 1)
+    xs = []
+    for i in range(n):
+        xs.append(F(b[i]) - sum(F(L[i, j]) * xs[j] for j in range(i)))
+    for i in range(n):
+        assert abs(F(out[7][i]) - xs[i]) <= F(np.spacing(abs(float(xs[i])))) / 2
+
+
+def test_double_word_keeps_nan_and_infinity():
+    """beta = 0 keeps a NaN of C (mscal multiplies) and an infinite input stays
+    infinite rather than turning into the NaN of a low-part cancellation."""
+    import oracle
+
+    C = np.array([np.nan, 1.0, 2.0, 3.0])
+    A = np.ones(4)
+    _, out = oracle.call_dw("dgemm", 101, 111, 111, 2, 2, 2, 1.0, A, 2, A, 2, 0.0, C, 2)
+    assert np.isnan(out[12][0]) and np.array_equal(out[12][1:], [2.0, 2.0, 2.0])
+    y = np.array([1.0, np.inf])
+    _, out = oracle.call_dw("daxpy", 2, 2.0, np.ones(2), 1, y, 1)
+    assert out[4][0] == 3.0 and out[4][1] == np.inf

@@ -1,11 +1,12 @@
 """Request server with continuous batching: every request of a mixed stream
 (gemm / gemv / trsv / syrk, single and double precision, served on several
 worker streams at once) must give the same bits as the same request served
-alone, and meet the oracle checks (1% rule and componentwise FP bound)."""
+alone, and meet the oracle checks (1% rule and componentwise FP bound, trsv
+by the residual bound)."""
 import numpy as np
 import pytest
 
-from common import LO, NT, NU, ROW, TR, UN, UP, Case, assert_rel1pct, check_case, run_oracle
+from common import LO, NT, NU, ROW, TR, UN, UP, Case, assert_rel1pct, check_case, run_oracle, trsv_residual_ok
 
 DT = {"s": np.float32, "d": np.float64}
 
@@ -111,6 +112,7 @@ def test_served_results_same_alone_and_in_mix(cuda):
         if c.op.endswith("trsv"):
             _, o_a = run_oracle(c)
             assert_rel1pct(mixed[i], o_a[c.outputs[0]], f"served {c}")
+            trsv_residual_ok(c, mixed[i])
         else:
             check_case(c, None, got, what="served")
 
