@@ -69,13 +69,30 @@ DevInfo &device_setup() {
   return d;
 }
 
+// Device or managed memory that the current device owns (a pointer into
+// another GPU's memory is refused rather than read as a peer access).
 bool on_device(const void *p) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice) return a.device == dev;
+  return a.type == cudaMemoryTypeManaged;
+}
+
+// y = beta * y, or y = 0 without reading y when beta == 0: what exo_sgemv's
+// scal does when x is empty (scal.py:9-19).
+__global__ void beta_scale_kernel(long n, float beta, float *y, long incy) {
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    float &v = y[i * incy];
+    v = beta == 0.0f ? 0.0f : beta * v;
+  }
 }
 
 size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -83,10 +100,20 @@ size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 }  // namespace
 
 // Same arithmetic and kernels as exo_sgemv (src/level2/gemv.py:10-22),
-// launched on the caller's stream without waiting.
+// launched on the caller's stream without waiting.  Column-major calls are
+// taken exactly when exo_sgemv takes them (exoblas_set_column_major).
 static void sgemv_noalloc(int order, int TransA, int M, int N, float alpha, const float *A, int lda, const float *X,
                           int incX, float beta, float *Y, int incY, cudaStream_t stream) {
   using namespace l2;
+  if (order == kColMajor && column_major_enabled()) {
+    // as exo_sgemv: a column-major M x N matrix is the row-major N x M
+    // matrix of its transpose
+    order = kRowMajor;
+    TransA = TransA == kNoTrans ? kTrans : kNoTrans;
+    const int t = M;
+    M = N;
+    N = t;
+  }
   if (order != kRowMajor) fail(EXOBLAS_UNSUPPORTED_ORDER, "Order must be CblasRowMajor");
   if (M < 0 || N < 0) fail(EXOBLAS_INVALID_VALUE, "M < 0 or N < 0");
   const bool trans = TransA != kNoTrans;
@@ -98,12 +125,13 @@ static void sgemv_noalloc(int order, int TransA, int M, int N, float alpha, cons
   if (incY < 0) Y = Y + (1 - ylen) * long(incY);
   DevInfo &d = device_setup();
   if (xlen == 0) {
-    // y = beta * y (gemv.py:13-14): the finish kernel with no partial sums
+    // y = beta * y (gemv.py:13-14); alpha is not used, so a NaN alpha does
+    // not reach y, as in exo_sgemv
     if (!on_device(Y)) fail(EXOBLAS_INVALID_VALUE, "exoblas_sgemv_noalloc takes device pointers only");
-    const long blocks = l2::finish_blocks(ylen, long(d.sm_count) * 8);
-    l2::finish_kernel<float, 0><<<int(blocks), l2::kThreads, 0, stream>>>(ylen, 0, nullptr, alpha, beta, Y, incY,
-                                                                         nullptr, false);
-    EXB_LAUNCH("partial-sum kernel");
+    long blocks = ceil_div(ylen, kThreads);
+    if (blocks > long(d.sm_count) * 4) blocks = long(d.sm_count) * 4;
+    beta_scale_kernel<<<int(blocks), kThreads, 0, stream>>>(ylen, beta, Y, incY);
+    EXB_LAUNCH("beta scale kernel");
     count_launch();
     return;
   }
@@ -126,6 +154,8 @@ static void sgemv_noalloc(int order, int TransA, int M, int N, float alpha, cons
     const long room = xbytes >= kNoAllocScratchBytes ? 0 : long((kNoAllocScratchBytes - xbytes) / (size_t(cols) * 4));
     if (room < 1)
       fail(EXOBLAS_INVALID_VALUE, "exoblas_sgemv_noalloc: problem exceeds the 4 MiB no-alloc scratch");
+    // fewer chunks than exo_sgemv would use when the array is short: the
+    // column sums then run in another order and can differ in the last bits
     chunks = int(want < room ? want : room);
   } else if (xbytes > kNoAllocScratchBytes) {
     fail(EXOBLAS_INVALID_VALUE, "exoblas_sgemv_noalloc: packed x exceeds the 4 MiB no-alloc scratch");

@@ -214,15 +214,20 @@ EXOBLAS_API void exo_dtrsv(const enum CBLAS_ORDER order, const enum CBLAS_UPLO U
  * callers that cannot allocate device memory (e.g. a plugin inside a
  * framework whose allocator owns all device memory, or a loop that must not
  * block in the driver's allocator).  Same arguments and arithmetic as
- * exo_sgemv plus a cudaStream_t (NULL: the legacy default stream); A, X and Y
- * must be device pointers.  The call queues its kernels and returns without
+ * exo_sgemv plus a cudaStream_t (NULL: the legacy default stream), and
+ * column-major calls are accepted exactly when exo_sgemv accepts them
+ * (exoblas_set_column_major); A, X and Y must be device pointers on the
+ * current device.  The call queues its kernels and returns without
  * waiting, and returns the status (also readable with exoblas_get_status).
  * It allocates nothing: its scratch is a fixed 4 MiB array inside the
  * library, held on every GPU that loads it.  Limit: a Trans call needs
  * 4*N bytes (one column-sum chunk) plus, when X is strided or not 16-byte
  * aligned, 4*M bytes for a packed copy of X; a NoTrans call with such an X
  * needs 4*N bytes; larger problems are rejected with EXOBLAS_INVALID_VALUE
- * before any work is queued.  Every call shares the array, so calls that
+ * before any work is queued.  A Trans call whose packed X leaves room for
+ * fewer column-sum chunks than exo_sgemv would use runs with fewer chunks,
+ * so its sums run in another order and can differ from exo_sgemv's in the
+ * last bits (both stay within the same error bound).  Every call shares the array, so calls that
  * overlap on the GPU race and must be serialised.  The first call on each
  * device looks the array's address up (cudaGetSymbolAddress); make it before
  * any stream capture starts on that device. */
