@@ -15,20 +15,26 @@ value      aggregate algorithmic GB/s (decimal) of the set, device-resident
            operands, kernels queued through the exo_* C ABI with device
            pointers (non-blocking mode, device-result reductions), timed with
            CUDA events on the library's stream.
-e2e        the same set through the same entry points with pinned HOST
-           buffers: the library stages every operand host->device and copies
-           outputs back inside the timed region (wall clock).  It also
-           carries this box's pinned copy rates and frac_of_link_bound: the
+e2e        the same set through the same entry points with pageable HOST
+           buffers (what a drop-in CBLAS caller passes): the library stages
+           every operand host->device and copies outputs back inside the
+           timed region (wall clock).  The pinned-buffer figure sits beside
+           it with this box's pinned copy rates and frac_of_link_bound: the
            time the copies alone (at those rates) plus the device step take,
-           over the measured e2e step.
+           over the measured pinned e2e step.
 roofline   the kernel with the largest share of the step, against the
            measured HBM copy bandwidth in MEASURED_PEAKS.json.
 cpu_baseline  the CPU oracle (C++ restatement of the reference algorithms,
-           threaded over ranges/rows) on a bounded sample of the same set.
-cpu_openblas  the same sample through SciPy's bundled OpenBLAS, the CBLAS
-           the reference compares against: one thread and all host threads.
+           threaded over ranges/rows) on the full set, all host cores,
+           measured by the --impl reference routine in a fresh process.
+cpu_openblas  the same set through SciPy's bundled OpenBLAS, the CBLAS the
+           reference compares against: one thread and all host threads.
+level3     configurations 1 and 3 measured in the same run: sgemm NN 1024^3
+           (alpha 1, beta 0.5, seed 0) with the oracle's CPU sgemm beside it,
+           and sgemm 8192^3 plain FFMA vs split-BF16 with their errors.
 
---impl reference times that CPU implementation alone on the host cores.
+--impl reference times that CPU implementation alone on the host cores:
+at least 1 s of warm-up, at least 1 s timed, the median pass.
 Multi-GPU: replicas only (one independent replica per rank, no collective).
 """
 from __future__ import annotations
@@ -74,6 +80,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-level3", action="store_true", help="skip the level-3 figures of the default line")
     ap.add_argument("--workload", choices=["bandwidth", "precision", "batch", "serve", "routines"],
                     default="bandwidth",
                     help="bandwidth: the level-1/2 set (default); precision: the level-3 precision set; batch: "
@@ -220,85 +227,115 @@ def host_launchers(L, H):
 
 
 # ----------------------------------------------------------- CPU baseline --
-SAMPLE = {  # bounded CPU sample of the same set (sizes divided down)
-    "saxpy": 1 << 24, "sdot": 1 << 24, "dsdot": 1 << 24, "daxpy": 1 << 23, "ddot": 1 << 23,
-    "sgemv_n": 8192, "sgemv_t": 8192, "dtrsv": 4096,
-}
-SAMPLE_SIZES = ("same set at reduced sizes: saxpy/sdot/dsdot n=2^24, daxpy/ddot n=2^23, sgemv N+T 8192^2, "
-                "dtrsv n=4096")
-SAMPLE_DESC = SAMPLE_SIZES + "; oracle_par_* drivers (C++ restatement of the reference algorithms, -O3)"
+# The reference's CPU path on the same workload: the full bandwidth set at the
+# sizes above (one pass = every kernel once), seeded uniform[-1, 1) inputs
+# generated on the host.  sgemv N and T read one shared matrix (each pass
+# streams it twice from DRAM all the same: 1 GiB is far beyond the caches).
+CPU_DESC = ("full bandwidth set (saxpy/sdot/dsdot n=2^26, daxpy/ddot n=2^25, sgemv N+T 16384^2, dtrsv n=8192) "
+            "through the oracle's threaded drivers (C++ restatement of the reference algorithms, -O3, "
+            "std::thread ranges, no pinning)")
+CPU_PROTOCOL = ">=1 s warm-up, >=1 s and >=3 passes timed, median pass (test/CMakeLists.txt:49-57)"
 
 
-def sample_bytes(k):
-    n = SAMPLE[k]
-    return {"saxpy": 12 * n, "sdot": 8 * n, "dsdot": 8 * n, "daxpy": 24 * n, "ddot": 16 * n,
-            "sgemv_n": (n * n + 3 * n) * 4, "sgemv_t": (n * n + 3 * n) * 4,
-            "dtrsv": (n * (n + 1) // 2 + 2 * n) * 8}[k]
-
-
-def cpu_sample_inputs():
+def cpu_inputs():
     import numpy as np
 
     g = np.random.default_rng(0)
-    u = lambda n, dt: g.uniform(-1, 1, n).astype(dt)
-    S = {}
-    for k in ("saxpy", "sdot", "dsdot"):
-        S[k] = (u(SAMPLE[k], np.float32), u(SAMPLE[k], np.float32))
-    for k in ("daxpy", "ddot"):
-        S[k] = (u(SAMPLE[k], np.float64), u(SAMPLE[k], np.float64))
-    for k in ("sgemv_n", "sgemv_t"):
-        n = SAMPLE[k]
-        S[k] = (u(n * n, np.float32), u(n, np.float32), u(n, np.float32))
-    n = SAMPLE["dtrsv"]
-    A = g.uniform(-1, 1, (n, n)) / n
-    A[np.arange(n), np.arange(n)] = 1.0 + g.uniform(0, 1, n)
-    S["dtrsv"] = (A.ravel().copy(), u(n, np.float64))
+
+    def u(n, dt):
+        v = g.random(n, dtype=dt)
+        v *= 2
+        v -= 1
+        return v
+
+    f, d = np.float32, np.float64
+    S = {"saxpy": (u(N1S, f), u(N1S, f)), "sdot": (u(N1S, f), u(N1S, f)), "dsdot": (u(N1S, f), u(N1S, f)),
+         "daxpy": (u(N1D, d), u(N1D, d)), "ddot": (u(N1D, d), u(N1D, d))}
+    Ag = u(NG * NG, f)
+    S["sgemv_n"] = (Ag, u(NG, f), u(NG, f))
+    S["sgemv_t"] = (Ag, u(NG, f), u(NG, f))
+    A = u(NT * NT, d).reshape(NT, NT)
+    A /= NT
+    A[np.arange(NT), np.arange(NT)] = 1.0 + g.random(NT)
+    S["dtrsv"] = (A.ravel(), u(NT, d))
     return S
 
 
-def cpu_step(S, threads):
-    """One pass of the sample through the oracle's threaded drivers; returns
-    per-kernel seconds."""
+def cpu_pass(S, threads):
+    """One pass of the set through the oracle's threaded drivers (threads > 0)
+    or through OpenBLAS (threads = 0, its own thread setting); returns seconds."""
     import oracle
 
-    t = {}
-    for k in SAMPLE:
-        n = SAMPLE[k]
+    t0 = time.perf_counter()
+    for k, _ in KERNELS:
         a = S[k]
-        t0 = time.perf_counter()
+        if threads <= 0:
+            from oracle import cblas
+
+            if k in ("saxpy", "daxpy"):
+                cblas.call(k, len(a[0]), 0.75, a[0], 1, a[1], 1)
+            elif k in ("sdot", "ddot", "dsdot"):
+                cblas.call(k, len(a[0]), a[0], 1, a[1], 1)
+            elif k in ("sgemv_n", "sgemv_t"):
+                cblas.call("sgemv", 101, 111 if k == "sgemv_n" else 112, NG, NG, 1.0, a[0], NG, a[1], 1, 0.5, a[2], 1)
+            else:
+                x = a[1].copy()
+                cblas.call("dtrsv", 101, 122, 111, 131, NT, a[0], NT, x, 1)
+            continue
         if k == "saxpy":
-            oracle.call("par_saxpy", threads, n, 0.75, a[0], a[1])
+            oracle.call("par_saxpy", threads, N1S, 0.75, a[0], a[1])
         elif k == "daxpy":
-            oracle.call("par_daxpy", threads, n, 0.75, a[0], a[1])
+            oracle.call("par_daxpy", threads, N1D, 0.75, a[0], a[1])
         elif k == "sdot":
-            oracle.call("par_sdot", threads, n, a[0], a[1])
+            oracle.call("par_sdot", threads, N1S, a[0], a[1])
         elif k == "ddot":
-            oracle.call("par_ddot", threads, n, a[0], a[1])
+            oracle.call("par_ddot", threads, N1D, a[0], a[1])
         elif k == "dsdot":
-            oracle.call("par_dsdot", threads, n, a[0], a[1])
-        elif k == "sgemv_n":
-            oracle.call("par_sgemv", threads, 111, n, n, 1.0, a[0], n, a[1], 0.5, a[2])
-        elif k == "sgemv_t":
-            oracle.call("par_sgemv", threads, 112, n, n, 1.0, a[0], n, a[1], 0.5, a[2])
-        elif k == "dtrsv":
+            oracle.call("par_dsdot", threads, N1S, a[0], a[1])
+        elif k in ("sgemv_n", "sgemv_t"):
+            oracle.call("par_sgemv", threads, 111 if k == "sgemv_n" else 112, NG, NG, 1.0, a[0], NG, a[1], 0.5, a[2])
+        else:
             x = a[1].copy()
-            oracle.call("par_dtrsv_lnn", threads, n, a[0], n, x)
-        t[k] = time.perf_counter() - t0
-    return t
+            oracle.call("par_dtrsv_lnn", threads, NT, a[0], NT, x)
+    return time.perf_counter() - t0
 
 
-def cpu_baseline(min_seconds=10.0):
-    threads = os.cpu_count() or 1
-    S = cpu_sample_inputs()
-    cpu_step(S, threads)  # warm-up
-    total_b, total_t, reps = 0, 0.0, 0
-    while total_t < min_seconds or reps < 2:
-        t = cpu_step(S, threads)
-        total_t += sum(t.values())
-        total_b += sum(sample_bytes(k) for k in SAMPLE)
-        reps += 1
-    return {"value": total_b / total_t / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{SAMPLE_DESC}; {reps} passes, {total_t:.1f} s"}
+def cpu_measure(S, threads, warm_passes=0, passes=0, warm_s=1.0, min_s=1.0):
+    """The reference's benchmark protocol on the host: warm up for at least
+    warm_s (and warm_passes passes), then time passes until at least min_s
+    and max(passes, 3) passes have run; GB/s of the median pass."""
+    t, w = 0.0, 0
+    while t < warm_s or w < warm_passes:
+        t += cpu_pass(S, threads)
+        w += 1
+    times = []
+    while sum(times) < min_s or len(times) < max(passes, 3):
+        times.append(cpu_pass(S, threads))
+    step_bytes = sum(BYTES.values())
+    med = statistics.median(times)
+    return {"value": round(step_bytes / med / 1e9, 3), "ms_per_pass": round(med * 1e3, 3), "passes": len(times),
+            "warmup_passes": w, "seconds": round(sum(times), 2),
+            "spread": [round(step_bytes / max(times) / 1e9, 3), round(step_bytes / min(times) / 1e9, 3)]}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline():
+    """The reference arm's own measurement (same routine, same sizes), run in
+    a fresh process so that it sees the host exactly as `--impl reference`
+    does (no CUDA context, no pinned buffers of this process)."""
+    r = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "reference", "--steps", "3",
+                        "--warmup", "1"], capture_output=True, text=True)
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"unavailable": f"reference arm exited {r.returncode}: {r.stderr.strip()[-300:]}"}
+    ref = json.loads(lines[-1])
+    return dict(ref["cpu_baseline"], ms_per_pass=ref["ms_per_step"], same_config=True)
 
 
 def host_link_rates(local, nbytes=1 << 30):
@@ -320,32 +357,10 @@ def host_link_rates(local, nbytes=1 << 30):
     return out[0], out[1]
 
 
-def openblas_step(S):
-    """One pass of the CPU sample through SciPy's bundled OpenBLAS (the CBLAS
-    the reference compares against); returns per-kernel seconds."""
-    from oracle import cblas
-
-    t = {}
-    for k in SAMPLE:
-        n = SAMPLE[k]
-        a = S[k]
-        t0 = time.perf_counter()
-        if k in ("saxpy", "daxpy"):
-            cblas.call(k, n, 0.75, a[0], 1, a[1], 1)
-        elif k in ("sdot", "ddot", "dsdot"):
-            cblas.call(k, n, a[0], 1, a[1], 1)
-        elif k in ("sgemv_n", "sgemv_t"):
-            cblas.call("sgemv", 101, 111 if k == "sgemv_n" else 112, n, n, 1.0, a[0], n, a[1], 1, 0.5, a[2], 1)
-        elif k == "dtrsv":
-            x = a[1].copy()
-            cblas.call("dtrsv", 101, 122, 111, 131, n, a[0], n, x, 1)
-        t[k] = time.perf_counter() - t0
-    return t
-
-
-def openblas_baseline(seconds_each=5.0):
-    """The same bounded sample as cpu_baseline through OpenBLAS, one thread
-    and all host threads (the reference's own comparison library)."""
+def openblas_baseline(S=None):
+    """The same full set through SciPy's bundled OpenBLAS (the CBLAS the
+    reference compares against), one thread and all host threads, with the
+    same protocol as cpu_measure."""
     try:
         from oracle import cblas
 
@@ -353,19 +368,13 @@ def openblas_baseline(seconds_each=5.0):
             return {"unavailable": "SciPy's bundled OpenBLAS not found"}
     except ImportError as e:
         return {"unavailable": f"oracle.cblas: {e}"}
-    S = cpu_sample_inputs()
-    out = {"unit": UNIT, "kind": "OpenBLAS bundled with SciPy (scipy_cblas_*)", "sample": SAMPLE_SIZES}
-    cores = os.cpu_count() or 1
+    S = S or cpu_inputs()
+    cores = cpu_threads()
+    out = {"unit": UNIT, "kind": "OpenBLAS bundled with SciPy (scipy_cblas_*)", "sample": "full bandwidth set",
+           "protocol": CPU_PROTOCOL, "cores": cores}
     for label, threads in (("one_thread", 1), ("all_threads", cores)):
         cblas.set_threads(threads)
-        openblas_step(S)  # warm-up
-        tb, tt = 0, 0.0
-        while tt < seconds_each:
-            t = openblas_step(S)
-            tt += sum(t.values())
-            tb += sum(sample_bytes(k) for k in SAMPLE)
-        out[label] = round(tb / tt / 1e9, 3)
-    out["cores"] = cores
+        out[label] = cpu_measure(S, 0)["value"]
     cblas.set_threads(1)
     return out
 
@@ -380,6 +389,106 @@ def max_over_ranks(dist, value, device):
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+# ------------------------------------------------------- level-3 figures --
+def level3_figures(L, eb, torch, stream, cpu=True):
+    """Level-3 configurations measured beside the bandwidth set.
+
+    sgemm_1024: sgemm NN 1024^3, lda = ldb = ldc = 1024, alpha 1, beta 0.5, A,
+    B, C uniform[-1, 1) from seed 0 (NumPy PCG64, float64 cast to float32):
+    device TFLOP/s over 2MNK + 3MN flops (CUDA events, mean of 50 calls after
+    5), the max / median componentwise relative error of one call against
+    FP64, and the oracle's sgemm (the reference algorithm, one thread and all
+    host threads) on the same inputs.
+    sgemm_8192: sgemm NN 8192^3 uniform[-1, 1), plain FP32 FFMA and
+    split-BF16 on tcgen05, TFLOP/s and error on 128 sampled rows against an
+    FP64 product on the device."""
+    import numpy as np
+
+    vp = C.c_void_p
+
+    def timed(fn, warm, reps):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if L.exoblas_synchronize() != 0:
+            raise RuntimeError("library failure in the level-3 figures")
+        return e0.elapsed_time(e1) / reps
+
+    def errs(got, ref, mag):
+        rel = ((got - ref).abs() / mag.clamp_min(1e-300)).flatten()
+        return {"max_rel_err": float(rel.max()), "median_rel_err": float(rel.median())}
+
+    out = {}
+    n = 1024
+    g = np.random.default_rng(0)
+    A = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    B = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    C0 = g.uniform(-1, 1, (n, n)).astype(np.float32)
+    dA, dB, dC0 = (torch.from_numpy(v).cuda() for v in (A, B, C0))
+    dC = dC0.clone()
+    torch.cuda.synchronize()
+    f = lambda: L.exo_sgemm(101, 111, 111, n, n, n, 1.0, vp(dA.data_ptr()), n, vp(dB.data_ptr()), n, 0.5,
+                            vp(dC.data_ptr()), n)
+    ms = timed(f, 5, 50)
+    dC.copy_(dC0)
+    torch.cuda.synchronize()
+    timed(f, 0, 1)
+    A64, B64, C64 = dA.double(), dB.double(), dC0.double()
+    flops1 = 2.0 * n ** 3 + 3.0 * n * n
+    out["sgemm_1024"] = {"config": "sgemm NN 1024^3 alpha 1 beta 0.5 seed 0", "ms": round(ms, 4),
+                         "tflops": round(flops1 / ms / 1e9, 2),
+                         **errs(dC.double(), A64 @ B64 + 0.5 * C64, A64.abs() @ B64.abs() + 0.5 * C64.abs())}
+    if cpu:
+        import oracle
+
+        threads = cpu_threads()
+        for label, th in (("cpu_port_one_thread", 1), ("cpu_port_all_threads", threads)):
+            Cc = C0.copy()
+            oracle.call("par_sgemm", th, 111, 111, n, n, n, 1.0, A, n, B, n, 0.5, Cc, n)  # warm-up
+            ts = []
+            while sum(ts) < 1.0 or len(ts) < 3:
+                Cc = C0.copy()
+                t0 = time.perf_counter()
+                oracle.call("par_sgemm", th, 111, 111, n, n, n, 1.0, A, n, B, n, 0.5, Cc, n)
+                ts.append(time.perf_counter() - t0)
+            med = statistics.median(ts)
+            out["sgemm_1024"][label] = {"ms": round(med * 1e3, 2), "tflops": round(flops1 / med / 1e12, 4),
+                                        "threads": th}
+    del dA, dB, dC, dC0, A64, B64, C64
+
+    n = 8192
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    A = (torch.rand(n, n, device="cuda", generator=gen, dtype=torch.float64) * 2 - 1).float()
+    B = (torch.rand(n, n, device="cuda", generator=gen, dtype=torch.float64) * 2 - 1).float()
+    rows = torch.arange(0, n, n // 128, device="cuda")
+    Ar, B64 = A[rows].double(), B.double()
+    ref, mag = Ar @ B64, Ar.abs() @ B64.abs()
+    del B64
+    res = {}
+    for mode, name in ((eb.PRECISION_NATIVE, "ffma"), (eb.PRECISION_SPLIT_BF16, "split_bf16")):
+        eb.set_precision(mode)
+        try:
+            Cg = torch.zeros(n, n, device="cuda")
+            f = lambda: L.exo_sgemm(101, 111, 111, n, n, n, 1.0, vp(A.data_ptr()), n, vp(B.data_ptr()), n, 0.0,
+                                    vp(Cg.data_ptr()), n)
+            ms = timed(f, 1, 3 if mode == eb.PRECISION_NATIVE else 6)
+        finally:
+            eb.set_precision(eb.PRECISION_NATIVE)
+        res[name] = {"ms": round(ms, 3), "tflops": round(2.0 * n ** 3 / ms / 1e9, 1),
+                     **errs(Cg[rows].double(), ref, mag)}
+        del Cg
+    res["speedup_split_over_ffma"] = round(res["split_bf16"]["tflops"] / res["ffma"]["tflops"], 2)
+    res["config"] = "sgemm NN 8192^3 uniform[-1,1), alpha 1 beta 0; error on 128 rows against FP64"
+    out["sgemm_8192"] = res
+    return out
 
 
 # ------------------------------------------------------------------- main --
@@ -482,42 +591,59 @@ def main():
                 "frac_of_measured_hbm": round(BYTES[k] / (per[k] * 1e-3) / 1e9 / hbm, 3),
                 "share": round(per[k] / sum(per.values()), 3)} for k in names}
 
-    # ---- end to end through the C ABI with pinned host buffers
+    # ---- end to end through the C ABI with host buffers: pageable memory
+    # (what a drop-in CBLAS caller hands over, the headline) and pinned
+    # memory (reported beside it)
     e2e = None
     if not args.no_e2e:
-        H = {k: tuple(t.cpu().pin_memory() for t in v) for k, v in X.items()}
-        hrun = host_launchers(L, H)
         eb.set_blocking(True)
-        for k in names:
-            hrun[k]()
-        h0, d0 = C.c_ulonglong(), C.c_ulonglong()
-        h1, d1 = C.c_ulonglong(), C.c_ulonglong()
-        KE = max(3, min(K, 20))
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        L.exoblas_staged_bytes(C.byref(h0), C.byref(d0))
-        t0 = time.perf_counter()
-        for _ in range(KE):
+
+        def e2e_run(H):
+            hrun = host_launchers(L, H)
             for k in names:
                 hrun[k]()
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        L.exoblas_staged_bytes(C.byref(h1), C.byref(d1))
-        if L.exoblas_get_status() != 0:
-            raise RuntimeError("library reported a failure in the e2e region")
-        e2e_s = t1 - t0
-        if dist:
-            e2e_s = max_over_ranks(dist, e2e_s, f"cuda:{local}")
-        h2d_step, d2h_step = (h1.value - h0.value) // KE, (d1.value - d0.value) // KE
+            h0, d0 = C.c_ulonglong(), C.c_ulonglong()
+            h1, d1 = C.c_ulonglong(), C.c_ulonglong()
+            KE = max(3, min(K, 20))
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            L.exoblas_staged_bytes(C.byref(h0), C.byref(d0))
+            t0 = time.perf_counter()
+            for _ in range(KE):
+                for k in names:
+                    hrun[k]()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            L.exoblas_staged_bytes(C.byref(h1), C.byref(d1))
+            if L.exoblas_get_status() != 0:
+                raise RuntimeError("library reported a failure in the e2e region")
+            e2e_s = t1 - t0
+            if dist:
+                e2e_s = max_over_ranks(dist, e2e_s, f"cuda:{local}")
+            return e2e_s, KE, (h1.value - h0.value) // KE, (d1.value - d0.value) // KE
+
+        Hpage = {k: tuple(t.cpu() for t in v) for k, v in X.items()}
+        e2e_s, KE, h2d_step, d2h_step = e2e_run(Hpage)
+        del Hpage
+        Hpin = {k: tuple(t.cpu().pin_memory() for t in v) for k, v in X.items()}
+        pin_s, KP, _, _ = e2e_run(Hpin)
+        del Hpin
         link_h, link_d = host_link_rates(local)
-        # time the host link alone would need per step (copies in, device
-        # work, copies out, one after another) over the measured step time
+        # time the pinned host link alone would need per step (copies in,
+        # device work, copies out, one after another) over the measured step
         ideal = h2d_step / (link_h * 1e9) + d2h_step / (link_d * 1e9) + ms_per_step * 1e-3
         e2e = {"value": round(world * step_bytes * KE / e2e_s / 1e9, 2), "unit": UNIT,
                "h2d_bytes_per_step": h2d_step, "d2h_bytes_per_step": d2h_step, "steps": KE,
-               "link_h2d_gbs": round(link_h, 1), "link_d2h_gbs": round(link_d, 1),
-               "frac_of_link_bound": round(ideal / (e2e_s / KE), 3)}
+               "host_memory": "pageable (torch CPU tensors, malloc-backed)",
+               "pinned": {"value": round(world * step_bytes * KP / pin_s / 1e9, 2), "steps": KP,
+                          "frac_of_link_bound": round(ideal / (pin_s / KP), 3)},
+               "link_h2d_gbs": round(link_h, 1), "link_d2h_gbs": round(link_d, 1)}
+
+    level3 = None
+    if rank == 0 and not args.no_level3:
+        with torch.cuda.stream(stream):
+            level3 = level3_figures(L, eb, torch, stream, cpu=not args.no_cpu_baseline)
 
     cpu = openblas = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -550,6 +676,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "kernels": kern,
+            "level3": level3,
         }
         print(json.dumps(line))
     if dist:
@@ -1058,25 +1185,23 @@ def serve_errors(torch, eb, call, stream, built, per_kind=12, max_work=1 << 30):
 
 
 def run_reference(args):
-    """The reference's CPU path (oracle port of the Exo algorithms) on all
-    host cores, each step one pass over the bounded sample."""
-    threads = os.cpu_count() or 1
-    S = cpu_sample_inputs()
-    for _ in range(args.warmup):
-        cpu_step(S, threads)
-    tot = 0.0
-    K = args.steps
-    for _ in range(K):
-        tot += sum(cpu_step(S, threads).values())
-    b = sum(sample_bytes(k) for k in SAMPLE)
-    v = K * b / tot / 1e9
+    """The reference's CPU path (the oracle's restatement of the Exo
+    algorithms, threaded over ranges / rows) on all host cores, over the full
+    bandwidth set: warm-up of max(--warmup passes, 1 s), then max(--steps
+    passes, 1 s) timed; value = the median pass."""
+    threads = cpu_threads()
+    S = cpu_inputs()
+    m = cpu_measure(S, threads, warm_passes=args.warmup, passes=args.steps)
+    v = m["value"]
+    cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": CPU_DESC,
+           "protocol": CPU_PROTOCOL, "passes": m["passes"], "seconds": m["seconds"], "spread": m["spread"]}
     line = {
-        "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-        "steps": K, "warmup": args.warmup, "ms_per_step": round(tot / K * 1e3, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": WORKLOAD, "sample": SAMPLE_DESC},
-        "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": threads, "kind": "port", "sample": SAMPLE_DESC},
-        "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": m["passes"], "warmup": m["warmup_passes"], "ms_per_step": m["ms_per_pass"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "impl": "reference", "config": {"workload": WORKLOAD, "sample": CPU_DESC, "same_config": True},
+        "cpu_baseline": cpu,
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
