@@ -54,6 +54,10 @@ struct Context {
   bool blocking = true;
   int precision = EXOBLAS_PRECISION_NATIVE;
   bool status_pending = false;  // a kernel with bounded waits was queued
+  // a second stream for work that runs beside the main stream's kernel (the
+  // extra streaming CTAs of the clustered trsv), joined back through events
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
   Arena scratch;      // partial sums, flags, counters (zeroed regions noted per kernel)
   Arena counters;     // small zero-initialised words; kernels leave them zero
   Arena staging[6];   // device copies of host operands, one slot per operand

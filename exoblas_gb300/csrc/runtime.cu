@@ -73,6 +73,9 @@ Context::~Context() {
   counters.release();
   for (auto &s : staging) s.release();
   if (own_stream && stream) cudaStreamDestroy(stream);
+  if (side) cudaStreamDestroy(side);
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
   cudaGetLastError();
 }
 

@@ -19,13 +19,19 @@
 //    barrier; with 16-CTA clusters (solve_chain2) dedicated critical and
 //    helper warps exchange through st.async stores counted on mbarriers.
 //    The operand rows the solver needs are prefetched with cp.async.
-//  * every other CTA STREAMS the bulk: work items (K, c) cover tiles
-//    L[K, J] for J in chunk c (kCT tiles) with J < K - kD, claimed in order of
-//    K (the step that needs them) through an atomic ticket.  An item writes
-//    its 64 partial row sums to slot (K, c) and sets the slot's flag; the
-//    solver adds the slots of block row K in slot order, so results are
-//    deterministic.
-//
+//    A 16-CTA solver CTA also has a publisher warp (x_m to global memory
+//    with its release flag) and a slot-loader warp (sums the streamers'
+//    slots of each block row ahead of time into shared memory), so no
+//    global-memory round trip sits on the helpers' loop.
+//  * every other CTA STREAMS the bulk, tiles L[K, J] with J < K - kD.  Row
+//    K's bulk is split into full chunks of kCT tiles and a tail holding its
+//    newest tiles; each work item writes its 64 partial row sums to its
+//    slot (K, c) and sets the slot's flag, and the solver adds the slots of
+//    block row K in slot order, so results are deterministic.  Tail workers
+//    (the first kTailCTAs of each streaming cluster) take tails in order of
+//    K, chunk workers take full chunks in order of readiness.  Extra
+//    streaming CTAs on a side stream use the SMs that the clusters leave
+//    free.
 // Deadlock freedom: the solver only waits on items, which are claimed in
 // order by running CTAs and themselves only wait on the solver's x flags;
 // streamers only wait on the solver, which is running.  Every wait is
@@ -50,17 +56,23 @@ namespace l2 {
 namespace tc {
 
 constexpr int kTB = 64;            // block size
-constexpr int kNT = 256;           // threads per CTA
-constexpr int kCT = 8;             // tiles per streamer chunk
+constexpr int kNT = 256;           // threads of a streaming CTA and of the 8-CTA solver
+constexpr int kNTS = 320;          // threads per CTA of a 16-CTA launch: 8 solver warps + publisher + slot loader
+constexpr int kCT = 4;             // tiles per streamer chunk
+static_assert(kCT <= 32, "one ballot bit per tile of an item");
+constexpr int kTailCTAs = 2;       // tail workers per streaming cluster
 constexpr int kD = 6;              // near tiles done by the solver: J = K-1 .. K-kD
 constexpr int kPre = 4;            // solver prefetch depth (steps)
 constexpr int kXR = 8;             // x ring depth (>= kD + 1)
 constexpr long long kSpin = 1ll << 24;
 
 template <typename T>
-struct SmemStream {
-  T tile[2][kTB][kTB + 1];
-  T zs[kCT][kTB];
+struct alignas(16) SmemStream {
+  // row pitch 64 + 64 / sizeof(T) elements: 16-byte row starts, and a row
+  // step of 4 mod 8 sixteen-byte bank groups (see stream_items)
+  static constexpr int kTP = kTB + 64 / int(sizeof(T));
+  T tile[3][kTB][kTP];  // three stages: tiles load two ahead of the one in use
+  alignas(16) T zs[kCT][kTB];  // x blocks of an item
 };
 
 template <typename T>
@@ -73,9 +85,10 @@ struct Args {
   T *slots;      // nb x nch x kTB
   int *xflag;    // nb
   int *sflag;    // nb x nch
-  int *ctl;      // [0] solver claim, [1] item ticket
+  int *ctl;      // [0] solver claim, [1] chunk ticket, [2] tail ticket, [3] resident clusters
   int *status;
   int nb, nch;
+  int nclusters;  // clusters of the clustered launch
   bool rev, trans, unit;
   bool vec16;  // rows of L are contiguous, 16-byte aligned runs of A (lower no-trans, even lda)
 };
@@ -132,42 +145,79 @@ __device__ __forceinline__ bool wait_flag(const int *p, int *status, bool &dead)
   return true;
 }
 
-// number of bulk chunks of block row K, and items before row K
-__device__ __host__ __forceinline__ int nch_row(long K) { return K > kD ? int((K - kD + kCT - 1) / kCT) : 0; }
-__device__ __host__ __forceinline__ long items_before(long K) {
-  const long M = K - 1 - kD;
+// Bulk of block row K (kD < K): tiles J < K - kD.  It splits into full
+// chunks c = 0 .. nfull(K)-1 of kCT tiles (J = kCT*c .. kCT*c + kCT-1) and a
+// tail of 1 .. kCT tiles ending at the newest tile J = K-kD-1.  The solver
+// adds the row's slots in order: its full chunks, then its tail.
+__device__ __host__ __forceinline__ int nfull(long K) { return K > kD ? int((K - kD - 1) / kCT) : 0; }
+__device__ __host__ __forceinline__ int nslots_row(long K) { return K > kD ? nfull(K) + 1 : 0; }
+// full chunks in groups c' < c, group c' holding chunk c' of every row that
+// has it (rows K >= kCT*(c'+1) + kD + 1), in increasing K
+__device__ __host__ __forceinline__ long chunks_in_groups_before(long c, long nb) {
+  const long M = nb - kCT - kD - 1;  // rows of group 0
   if (M <= 0) return 0;
-  const long q = M / kCT, r = M % kCT;
-  return kCT * q * (q + 1) / 2 + r * (q + 1);
+  const long imax = (M + kCT - 1) / kCT;
+  const long cc = c < imax ? c : imax;
+  return cc * M - kCT * cc * (cc - 1) / 2;
 }
+__device__ __host__ __forceinline__ long chunk_items(long nb) { return chunks_in_groups_before(nb, nb); }
+__device__ __host__ __forceinline__ long tail_items(long nb) { return nb - 1 - kD > 0 ? nb - 1 - kD : 0; }
 
 // ------------------------------------------------------------ streamers ----
+// Two kinds of streaming CTA.  Tail workers (the first kTailCTAs of every
+// streaming cluster) take the rows' tails in order of K: the tail of row K
+// holds the newest tiles, needed kD steps after x_{K-kD-1} appears, and a
+// tail worker computes each tile as soon as its x block is published.
+// Chunk workers take full chunks in order of the step that makes them ready
+// (chunk c is ready once x_{kCT*c + kCT-1} is published; within a group, rows
+// in increasing K).  A full chunk is never among a row's newest tiles, so a
+// chunk worker that waits for x holds nothing urgent.  (Claiming whole rows'
+// bulk in row order instead makes the work grow towards the end of the
+// solve, where every row has the most tiles.)
+__device__ __forceinline__ void chunk_of(long t, long nb, long &K, int &c) {
+  long lo = 0, hi = (nb - kD - 1) / kCT > 1 ? (nb - kD - 1) / kCT : 1;
+  while (lo < hi) {
+    const long mid = (lo + hi + 1) / 2;
+    if (chunks_in_groups_before(mid, nb) <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  c = int(lo);
+  K = kCT * (lo + 1) + kD + 1 + (t - chunks_in_groups_before(lo, nb));
+}
+
+// The first kNT threads of a streaming CTA (a 16-CTA launch has kNTS
+// threads; the extra warps of a streaming CTA return at once).
+__device__ __forceinline__ void work_sync() { asm volatile("bar.sync 2, 256;" ::: "memory"); }
+
 template <typename T>
-__device__ void stream_items(const Args<T> &a, SmemStream<T> &S, bool &dead) {
+__device__ void stream_items(const Args<T> &a, SmemStream<T> &S, bool &dead, bool tail_worker) {
   __shared__ long s_item;
-  const int tid = threadIdx.x;
-  const long total = items_before(a.nb);
+  __shared__ unsigned s_ready;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const long nb = a.nb;
+  const long total = tail_worker ? tail_items(nb) : chunk_items(nb);
+  int *ticket = a.ctl + (tail_worker ? 2 : 1);
   const int i = tid >> 2, q = tid & 3;  // row, quarter of the tile product
   for (;;) {
-    __syncthreads();
-    if (tid == 0) s_item = atomicAdd(a.ctl + 1, 1);
-    __syncthreads();
+    work_sync();
+    if (tid == 0) s_item = atomicAdd(ticket, 1);
+    work_sync();
     const long t = s_item;
     if (t >= total) return;
-    // item t -> (K, c): largest K with items_before(K) <= t
-    long lo = kD + 1, hi = a.nb - 1;
-    while (lo < hi) {
-      const long mid = (lo + hi + 1) / 2;
-      if (items_before(mid) <= t) lo = mid;
-      else hi = mid - 1;
+    long K, J0, J1;
+    int c;
+    if (tail_worker) {
+      K = kD + 1 + t;
+      c = nfull(K);
+      J0 = long(c) * kCT;
+      J1 = K - kD;
+    } else {
+      chunk_of(t, nb, K, c);
+      J0 = long(c) * kCT;
+      J1 = J0 + kCT;
     }
-    const long K = lo;
-    const int c = int(t - items_before(K));
-    const long J0 = long(c) * kCT;
-    long J1 = J0 + kCT;
-    if (J1 > K - kD) J1 = K - kD;
     const int ntiles = int(J1 - J0);
-    // stage tile J0 (and J0+1) with cp.async; element (r, cc) = L(K*64+r, J*64+cc)
+    // stage tiles J0, J0+1 with cp.async; element (r, cc) = L(K*64+r, J*64+cc)
     auto issue = [&](int slot, long J) {
       for (int e = tid; e < kTB * kTB; e += kNT) {
         // consecutive threads walk along A's contiguous dimension
@@ -180,35 +230,73 @@ __device__ void stream_items(const Args<T> &a, SmemStream<T> &S, bool &dead) {
       }
       cp_commit();
     };
-    T acc = 0;
     issue(0, J0);
+    if (ntiles > 1) issue(1, J0 + 1);
+    else cp_commit();  // one group per tile slot
+    // which x blocks of the item are published already: one poll for the
+    // whole item, then one round of loads for those x values
+    if (tid < 32) {
+      const int f = lane < ntiles ? ld_acquire(a.xflag + J0 + lane) : 0;
+      const unsigned m = __ballot_sync(0xffffffffu, f != 0);
+      if (lane == 0) s_ready = m;
+    }
+    work_sync();
+    const unsigned ready = s_ready;
+    for (int e = tid; e < ntiles * kTB; e += kNT) {
+      const int tt = e / kTB;
+      if ((ready >> tt) & 1u) {
+        const long gj = (J0 + tt) * kTB + e % kTB;
+        S.zs[tt][e % kTB] = gj < a.n ? __ldcg(a.z + zidx(a, gj)) : T(0);
+      }
+    }
+    // Tile product: thread (i, q) takes row i and the column pairs
+    // p = q + 4v (v = 0..7) as 16-byte loads, with two independent
+    // accumulators (even and odd v).  With the 72-element row pitch the eight
+    // lanes of a quarter-warp (rows i, i+1; q = 0..3) read eight different
+    // 16-byte bank groups, so the loads are conflict-free.
+    using V2 = typename V16<T>::type;
+    constexpr int kVE = int(16 / sizeof(T));  // elements per 16-byte load
+    constexpr int kNV = kTB / (4 * kVE);      // loads per thread and tile
+    T acc = 0, acc1 = 0;
     for (int tt = 0; tt < ntiles; ++tt) {
       const long J = J0 + tt;
-      if (tt + 1 < ntiles) issue((tt + 1) & 1, J + 1);
+      cp_wait<1>();  // tile tt has landed; tile tt+1 may be in flight
+      work_sync();   // ... for every thread, and tile tt-1 is no longer read
+      if (tt + 2 < ntiles) issue((tt + 2) % 3, J + 2);
       else cp_commit();  // keep one group per iteration
-      // x_J must be published by the solver
-      if (tid == 0) wait_flag(a.xflag + J, a.status, dead);
-      __syncthreads();
-      if (tid < kTB) {
-        const long gj = J * kTB + tid;
-        S.zs[tt][tid] = gj < a.n ? __ldcg(a.z + zidx(a, gj)) : T(0);
+      if (!((ready >> tt) & 1u)) {
+        // x_J was not published at the claim: wait for the solver
+        if (tid == 0) wait_flag(a.xflag + J, a.status, dead);
+        work_sync();
+        if (tid < kTB) {
+          const long gj = J * kTB + tid;
+          S.zs[tt][tid] = gj < a.n ? __ldcg(a.z + zidx(a, gj)) : T(0);
+        }
+        work_sync();
       }
-      cp_wait<1>();
-      __syncthreads();
-      const int slot = tt & 1;
+      const T *row = &S.tile[tt % 3][i][0];
+      const T *xv = &S.zs[tt][0];
 #pragma unroll
-      for (int jj = 0; jj < kTB / 4; ++jj) {
-        const int j = q * (kTB / 4) + jj;
-        acc = fma(S.tile[slot][i][j], S.zs[tt][j], acc);
+      for (int v = 0; v < kNV; ++v) {
+        const int col = (q + 4 * v) * kVE;
+        const V2 l = *reinterpret_cast<const V2 *>(row + col);
+        const V2 x = *reinterpret_cast<const V2 *>(xv + col);
+        if constexpr (sizeof(T) == 8) {
+          if (v & 1) acc1 = fma(l.y, x.y, fma(l.x, x.x, acc1));
+          else acc = fma(l.y, x.y, fma(l.x, x.x, acc));
+        } else {
+          if (v & 1) acc1 = fma(l.w, x.w, fma(l.z, x.z, fma(l.y, x.y, fma(l.x, x.x, acc1))));
+          else acc = fma(l.w, x.w, fma(l.z, x.z, fma(l.y, x.y, fma(l.x, x.x, acc))));
+        }
       }
-      __syncthreads();
     }
+    acc += acc1;
     cp_wait<0>();
     acc += __shfl_xor_sync(0xffffffffu, acc, 1);
     acc += __shfl_xor_sync(0xffffffffu, acc, 2);
     if (q == 0) a.slots[(K * a.nch + c) * kTB + i] = acc;
     __threadfence();
-    __syncthreads();
+    work_sync();
     if (tid == 0) st_release(a.sflag + K * a.nch + c, 1);
   }
 }
@@ -292,7 +380,7 @@ __device__ void solve_chain(const Args<T> &a, SmemSolver<T, CS> &S, bool &dead) 
     pend = 0;
     pend_nc = 0;
     if (K2 >= nb) return;
-    const int nc = nch_row(K2);
+    const int nc = nslots_row(K2);
     if (nc == 0) return;
     if (warp == 0 && !dead) {
       long long spins = 0;
@@ -321,7 +409,7 @@ __device__ void solve_chain(const Args<T> &a, SmemSolver<T, CS> &S, bool &dead) 
 
   for (int p = 0; p < kPre; ++p) prefetch(p);
   if (tid < RPC) S.carry[tid] = T(0);
-  // bulk of rows 0 and 1 is empty (nch_row(K) = 0 for K <= kD)
+  // bulk of rows 0 and 1 is empty (nslots_row(K) = 0 for K <= kD)
   request_slots(1);
   for (long K = 0; K < nb; ++K) {
     const int sidx = int(K % kPre);
@@ -430,6 +518,9 @@ __device__ void solve_chain(const Args<T> &a, SmemSolver<T, CS> &S, bool &dead) 
 // E2 phase K, i.e. after the critical warps consumed phase K.
 constexpr int kCS2 = 16;
 constexpr int kRPC2 = kTB / kCS2;  // 4
+constexpr int kSR = 4;                     // slot-sum ring depth (block rows)
+constexpr int kPubWarp = kNT / 32;         // warp 8
+constexpr int kLoaderWarp = kNT / 32 + 1;  // warp 9
 constexpr long long kWaitCycles = 4ll << 30;
 
 template <typename T>
@@ -440,9 +531,13 @@ struct SmemSolver2 {
   T rfull[2][kTB];
   T xring[kXR][kTB];
   T carry[2][kRPC2][32];  // per-lane partial sums of the carry, added inside the critical row dot
+  T slotsum[kSR][kRPC2];  // bulk sums of the owned rows, ring of kSR block rows (slot loader -> helpers)
   unsigned long long e1bar[2];
   unsigned long long e2bar[4];
   unsigned long long cready[2];
+  int pub_done;    // x_0 .. x_{pub_done-1} published to global memory (publisher -> helpers)
+  int slot_ready;  // slotsum holds block row slot_ready and the rows before it (slot loader -> helpers)
+  int slot_used;   // helpers have consumed the slot sums of rows up to slot_used (helpers -> slot loader)
 };
 
 __device__ __forceinline__ uint32_t sh_u32(const void *p) {
@@ -505,6 +600,28 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, int *sta
   }
 }
 __device__ __forceinline__ void helper_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ int ld_acquire_cta(const int *p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(sh_u32(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta(int *p, int v) {
+  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(sh_u32(p)), "r"(v) : "memory");
+}
+// Bounded wait, by a whole warp, for the shared counter *p to reach `want`.
+__device__ __forceinline__ bool wait_count(const int *p, int want, int *status, bool &dead) {
+  if (dead) return false;
+  const long long t0 = clock64();
+  for (;;) {
+    if (__all_sync(0xffffffffu, ld_acquire_cta(p) >= want)) return true;
+    if (__shfl_sync(0xffffffffu, int(clock64() - t0 > kWaitCycles), 0)) {
+      if ((threadIdx.x & 31) == 0) atomicExch(status, 1);
+      dead = true;
+      return false;
+    }
+    __nanosleep(32);
+  }
+}
 
 template <typename T>
 __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
@@ -523,6 +640,9 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     for (int i = 0; i < 2; ++i) arm(sh_u32(&S.e1bar[i]), kXBytes);
     for (int i = 0; i < 4; ++i) arm(sh_u32(&S.e2bar[i]), kXBytes);
+    S.pub_done = 0;
+    S.slot_ready = -1;
+    S.slot_used = kD;  // rows 0 .. kD have no bulk part
   }
   cl.sync();  // every barrier of the cluster is initialised before any remote arrive
 
@@ -560,7 +680,7 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
       if (lane < CS)
         st_async(map_rank(sh_u32(&S.xring[K % kXR][R * RPC + w]), lane), xk, map_rank(sh_u32(&S.e2bar[K & 3]), lane));
     }
-  } else {
+  } else if (warp < kNT / 32) {
     // ---------------- helper warps: warp RPC + h prepares row h's carry
     const int h = warp - RPC;
     const int ht = tid - RPC * 32;  // 0 .. 127
@@ -612,41 +732,31 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
       }
       cp_commit();
     };
-    // x_m to global memory and its flag (one warp; the publishing CTA rotates)
-    auto publish = [&](long m) {
-      for (int t = lane; t < kTB; t += 32) {
-        const long gi = m * kTB + t;
-        if (gi < n) a.z[zidx(a, gi)] = S.xring[m % kXR][t];
-      }
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) st_release(a.xflag + m, 1);
-    };
     for (int p = 0; p < kPre; ++p) prefetch(p);
     cp_wait<kPre - 1>();
     helper_sync();
     S.carry[0][h][lane] = T(0);
     arrive_local(sh_u32(&S.cready[0]));
-    // bulk slots of the row being prepared, loaded one iteration ahead so
-    // the loads are in flight while other work runs (lane c: slots c, c + 32)
-    T p0 = T(0), p1 = T(0), pmore = T(0);
     // Iteration T1 prepares the carry of step T1.  It starts when x_{T1-2}
-    // is exchanged: the stage of step T1-2 is then free for step T1-2+kPre
-    // and x_{T1-2} can be published; the carry (near tiles up to x_{T1-2}
-    // and the bulk slots) follows at once, the poll for the next row's bulk
-    // slots last.
+    // is exchanged: the stage of step T1-2 is then free for step T1-2+kPre;
+    // the carry is the near tiles up to x_{T1-2} plus the bulk sums of row
+    // T1, which the slot loader has summed into slotsum ahead of time.
     for (long T1 = 1; T1 < nb; ++T1) {
       if (T1 >= 2) {
         bar_wait(sh_u32(&S.e2bar[(T1 - 2) & 3]), uint32_t(((T1 - 2) >> 2) & 1), a.status, dead);
         prefetch(T1 - 2 + kPre);
-        if (h == RPC - 1 && (T1 - 2) % CS == R) publish(T1 - 2);
       } else {
         cp_commit();  // one group per iteration
       }
+      // The publisher must keep within three steps: the e2bar ring (4) and
+      // the x ring (8) it reads stay unaliased while step T1 waits for it.
+      wait_count(&S.pub_done, int(T1 - 3), a.status, dead);
       // groups so far: stages 0..kPre-1, one empty, then stage g-1 in group
       // g; stage T1 is complete once at most two groups are outstanding
       cp_wait<kPre - 2>();
       helper_sync();
+      // every helper has finished iteration T1-1: slot sums up to row T1-1 consumed
+      if (h == 0 && lane == 0 && T1 - 1 > kD) st_release_cta(&S.slot_used, int(T1 - 1));
       const T *st = S.stage[T1 % kPre];
       T s0 = T(0), s1 = T(0);
       for (int j = 1; j < kD; ++j) {
@@ -657,48 +767,101 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
         s0 = fma(row[lane], xv[lane], s0);
         s1 = fma(row[lane + 32], xv[lane + 32], s1);
       }
-      S.carry[T1 & 1][h][lane] = (s0 + s1) + ((p0 + p1) + pmore);
-      arrive_local(sh_u32(&S.cready[T1 & 1]));
-      // bulk slots of row T1 + 1, added in the next iteration
-      p0 = p1 = pmore = T(0);
-      const long K2 = T1 + 1;
-      const int nc = K2 < nb ? nch_row(K2) : 0;
-      if (nc > 0 && !dead) {
-        const long long t0 = clock64();
-        for (;;) {
-          int ok = 1;
-          for (int cc = lane; cc < nc; cc += 32) ok &= ld_acquire(a.sflag + K2 * a.nch + cc) != 0;
-          if (__all_sync(0xffffffffu, ok)) break;
-          if (__shfl_sync(0xffffffffu, int(clock64() - t0 > kWaitCycles), 0)) {
-            if (lane == 0) atomicExch(a.status, 1);
-            dead = true;
-            break;
-          }
-        }
-        const T *sl = a.slots + (K2 * a.nch) * kTB + R * RPC + h;
-        if (lane < nc) p0 = __ldcg(sl + long(lane) * kTB);
-        if (lane + 32 < nc) p1 = __ldcg(sl + long(lane + 32) * kTB);
-        for (int cc = lane + 64; cc < nc; cc += 32) pmore += __ldcg(sl + long(cc) * kTB);
+      T bulk = T(0);
+      if (nslots_row(T1) > 0) {
+        wait_count(&S.slot_ready, int(T1), a.status, dead);
+        bulk = S.slotsum[T1 % kSR][h];
       }
-    }
-    // the last two blocks
-    for (long m = nb - 2 < 0 ? 0 : nb - 2; m < nb; ++m) {
-      bar_wait(sh_u32(&S.e2bar[m & 3]), uint32_t((m >> 2) & 1), a.status, dead);
-      if (h == RPC - 1 && m % CS == R) publish(m);
+      S.carry[T1 & 1][h][lane] = (s0 + s1) + (lane == 0 ? bulk : T(0));
+      arrive_local(sh_u32(&S.cready[T1 & 1]));
     }
     cp_wait<0>();
+  } else if (warp == kPubWarp) {
+    // ---------------- publisher: x_m to global memory and its release flag,
+    // by the CTA m % CS, as soon as x_m is exchanged
+    for (long m = 0; m < nb; ++m) {
+      bar_wait(sh_u32(&S.e2bar[m & 3]), uint32_t((m >> 2) & 1), a.status, dead);
+      if (m % CS == R) {
+        for (int t = lane; t < kTB; t += 32) {
+          const long gi = m * kTB + t;
+          if (gi < n) a.z[zidx(a, gi)] = S.xring[m % kXR][t];
+        }
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) st_release(a.xflag + m, 1);
+      }
+      __syncwarp();
+      if (lane == 0) st_release_cta(&S.pub_done, int(m + 1));
+    }
+  } else if (warp == kLoaderWarp) {
+    // ---------------- slot loader: for block rows in order, wait for the
+    // streamers' slots, sum the owned rows' slots (lane l: row l / 8, slots
+    // l % 8, l % 8 + 8, ... in slot order, then a fixed tree over the eight
+    // lanes of the row) and hand the sums to the helpers through slotsum.
+    const int r = lane >> 3, q = lane & 7;
+    // one poll of row m's slot flags; true when all are set
+    auto flags_ready = [&](long m) -> bool {
+      const int nc = nslots_row(m);
+      int ok = 1;
+      for (int cc = lane; cc < nc; cc += 32) ok &= ld_acquire(a.sflag + m * a.nch + cc) != 0;
+      return __all_sync(0xffffffffu, ok) != 0;
+    };
+    auto wait_flags = [&](long m, bool seen) {
+      if (dead || seen) return;
+      const long long t0 = clock64();
+      while (!flags_ready(m)) {
+        if (__shfl_sync(0xffffffffu, int(clock64() - t0 > kWaitCycles), 0)) {
+          if (lane == 0) atomicExch(a.status, 1);
+          dead = true;
+          return;
+        }
+      }
+    };
+    bool next_seen = false;
+    for (long m = kD + 1; m < nb; ++m) {
+      const int nc = nslots_row(m);
+      wait_count(&S.slot_used, int(m - kSR), a.status, dead);  // row m - kSR consumed
+      wait_flags(m, next_seen);
+      // row m's slot loads in flight while row m+1's flags are polled once;
+      // each lane's slots in batches of eight independent loads, added in
+      // slot order
+      T v = T(0);
+      const T *sl = a.slots + (m * a.nch) * kTB + R * RPC + r;
+      T w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) w[u] = q + 8 * u < nc ? __ldcg(sl + long(q + 8 * u) * kTB) : T(0);
+      next_seen = m + 1 < nb && !dead && flags_ready(m + 1);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v += w[u];
+      for (int c0 = q + 64; c0 < nc; c0 += 64) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = c0 + 8 * u < nc ? __ldcg(sl + long(c0 + 8 * u) * kTB) : T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v += w[u];
+      }
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (q == 0) S.slotsum[m % kSR][r] = v;
+      __syncwarp();
+      __threadfence_block();
+      if (lane == 0) st_release_cta(&S.slot_ready, int(m));
+    }
   }
   cl.sync();  // no CTA leaves while a peer may still write into its shared memory
 }
 
 template <typename T, int CS>
-__global__ void __launch_bounds__(kNT, 1) trsv_cluster_kernel(Args<T> a) {
+__global__ void __launch_bounds__(kNTS, 1) trsv_cluster_kernel(Args<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cg::cluster_group cl = cg::this_cluster();
   __shared__ int s_role;
   // role: rank 0 of each cluster tries to claim the solver role
   if (threadIdx.x == 0) s_role = 0;
-  if (cl.block_rank() == 0 && threadIdx.x == 0) s_role = atomicCAS(a.ctl, 0, 1) == 0 ? 1 : 0;
+  if (cl.block_rank() == 0 && threadIdx.x == 0) {
+    s_role = atomicCAS(a.ctl, 0, 1) == 0 ? 1 : 0;
+    atomicAdd(a.ctl + 3, 1);  // this cluster is resident
+  }
   cl.sync();
   const int role = *cl.map_shared_rank(&s_role, 0);
   cl.sync();
@@ -708,8 +871,42 @@ __global__ void __launch_bounds__(kNT, 1) trsv_cluster_kernel(Args<T> a) {
       solve_chain2<T>(a, *reinterpret_cast<SmemSolver2<T> *>(smem_raw), dead);
     else
       solve_chain<T, CS>(a, *reinterpret_cast<SmemSolver<T, CS> *>(smem_raw), dead);
-  } else
-    stream_items<T>(a, *reinterpret_cast<SmemStream<T> *>(smem_raw), dead);
+  } else if (threadIdx.x < kNT) {  // a 16-CTA launch's extra warps have no streaming work
+    stream_items<T>(a, *reinterpret_cast<SmemStream<T> *>(smem_raw), dead, int(cl.block_rank()) < kTailCTAs);
+  }
+}
+
+// Extra streaming CTAs, launched on a side stream beside the clustered
+// launch to use the SMs that its clusters leave free (16-CTA clusters
+// occupy whole GPC partitions; the remainder of each GPC would idle).  They
+// take chunk items only, and only once every cluster of the clustered launch
+// is resident (each counts itself in ctl[3] as it starts).  The clustered
+// launch can then finish all the work by itself, so the extra CTAs only
+// speed it up and can never hold an SM that a cluster still needs: a CTA
+// that finds the clusters incomplete waits at most kExtraWaitNs and leaves.
+// Their shared memory is as large as a clustered CTA's, so none of them
+// shares an SM with a solver CTA.
+constexpr unsigned long long kExtraWaitNs = 20000;
+template <typename T>
+__global__ void __launch_bounds__(kNT, 1) trsv_extra_stream_kernel(Args<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_go;
+  if (threadIdx.x == 0) {
+    unsigned long long t0, t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    int go = ld_acquire(a.ctl + 3) >= a.nclusters;
+    while (!go) {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (t - t0 > kExtraWaitNs) break;
+      __nanosleep(256);
+      go = ld_acquire(a.ctl + 3) >= a.nclusters;
+    }
+    s_go = go;
+  }
+  __syncthreads();
+  if (!s_go) return;
+  bool dead = false;
+  stream_items<T>(a, *reinterpret_cast<SmemStream<T> *>(smem_raw), dead, false);
 }
 
 // ------------------------------------------------- diagonal-block inverse --
@@ -846,6 +1043,7 @@ static int max_clusters(cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr) {
   }
   attr[0].val.clusterDim.x = CS;
   cfg.dynamicSmemBytes = smem;
+  cfg.blockDim = dim3(CS == tc::kCS2 ? tc::kNTS : tc::kNT);
   cfg.gridDim = dim3(CS * 32);
   int m = 0;
   if (cudaOccupancyMaxActiveClusters(&m, kern, &cfg) != cudaSuccess) {
@@ -862,7 +1060,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   using namespace tc;
   Context &c = ctx();
   const int nb = int(ceil_div(n, kTB));
-  const int nch = nch_row(nb - 1) > 0 ? nch_row(nb - 1) : 1;
+  const int nch = nslots_row(nb - 1) > 0 ? nslots_row(nb - 1) : 1;
   // cluster size: 16 where two or more such clusters fit, else 8 (cached per device)
   static int cs_cache[64] = {0};
   static int mc_cache[64] = {0};
@@ -892,18 +1090,19 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   const int CS = cs_cache[dev];
   const long maxc = mc_cache[dev];
   if (maxc < 1) return false;
-  const long items = items_before(nb);
+  const long items = chunk_items(nb) + tail_items(nb);
   long clusters = 1 + ceil_div(items, CS);
   if (clusters > maxc) clusters = maxc;
   if (items > 0 && clusters < 2) return false;  // the solver needs streamers
   attr[0].val.clusterDim.x = CS;
+  cfg.blockDim = dim3(CS == kCS2 ? kNTS : kNT);
   cfg.dynamicSmemBytes = CS == 16 ? trsv_cluster_smem<T, 16>() : trsv_cluster_smem<T, 8>();
   cfg.gridDim = dim3(unsigned(clusters * CS));
 
   // scratch: inverses, slots, flags, control words
   const size_t inv_b = (size_t(nb) * kTB * kTB * sizeof(T) + 255) & ~size_t(255);
   const size_t slot_b = (size_t(nb) * nch * kTB * sizeof(T) + 255) & ~size_t(255);
-  const size_t flag_b = (size_t(nb) * (1 + nch) + 2) * 4;
+  const size_t flag_b = (size_t(nb) * (1 + nch) + 4) * 4;
   char *base = static_cast<char *>(scratch(inv_b + slot_b + flag_b));
   Args<T> a;
   a.n = n;
@@ -918,6 +1117,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   a.status = device_status_word();
   a.nb = nb;
   a.nch = nch;
+  a.nclusters = int(clusters);
   a.rev = upper != trans;
   a.trans = trans;
   a.unit = unit;
@@ -925,11 +1125,37 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   EXB_CUDA(cudaMemsetAsync(a.xflag, 0, flag_b, c.stream));
   trsv_inverse_kernel<T><<<nb, kNT, 0, c.stream>>>(a);
   EXB_LAUNCH("trsv inverse kernel");
+  // SMs the clustered launch leaves free, when it is at its size limit
+  const long extra = clusters == maxc ? long(c.sm_count) - clusters * CS : 0;
+  const bool use_extra = extra > 0 && chunk_items(nb) > 0;
+  if (use_extra) {
+    if (!c.side) {
+      EXB_CUDA(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+      EXB_CUDA(cudaEventCreateWithFlags(&c.fork, cudaEventDisableTiming));
+      EXB_CUDA(cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming));
+    }
+    // the side stream starts where the clustered launch starts
+    EXB_CUDA(cudaEventRecord(c.fork, c.stream));
+    EXB_CUDA(cudaStreamWaitEvent(c.side, c.fork, 0));
+  }
   if (CS == 16)
     EXB_CUDA(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T, 16>, a));
   else
     EXB_CUDA(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T, 8>, a));
   count_launch(2);
+  if (use_extra) {
+    const size_t smem = CS == 16 ? trsv_cluster_smem<T, 16>() : trsv_cluster_smem<T, 8>();
+    static std::once_flag attr_set[64];
+    std::call_once(attr_set[dev], [&] {
+      EXB_CUDA(cudaFuncSetAttribute(trsv_extra_stream_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(smem)));
+    });
+    trsv_extra_stream_kernel<T><<<unsigned(extra), kNT, smem, c.side>>>(a);
+    EXB_LAUNCH("trsv extra streaming kernel");
+    count_launch();
+    EXB_CUDA(cudaEventRecord(c.join, c.side));
+    EXB_CUDA(cudaStreamWaitEvent(c.stream, c.join, 0));
+  }
   c.status_pending = true;
   return true;
 }
