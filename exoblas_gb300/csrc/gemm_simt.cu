@@ -9,6 +9,8 @@
 // Reference algorithms: src/level3/{gemm,symm,syrk,syr2k,trmm}.py.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "runtime.h"
@@ -64,14 +66,21 @@ struct Tri {  // op(A) for a triangular A: zero outside the stored triangle, one
   __device__ __forceinline__ bool contiguous_cols() const { return !trans; }
 };
 
-template <typename T>
+// Tile configurations: 128x128 (8x8 per thread) for FP32, 64x64 (4x4 per
+// thread) for FP64 and for FP32 products too small to give every SM a
+// 128x128 tile (sgemm 1024^3 has 64 such tiles for 152 SMs, 256 of 64x64).
+template <typename T, bool SMALL = false>
 struct Cfg;
 template <>
-struct Cfg<float> {
+struct Cfg<float, false> {
   static constexpr int BM = 128, BN = 128, BK = 16, TM = 8, TN = 8, THREADS = 256;
 };
 template <>
-struct Cfg<double> {
+struct Cfg<float, true> {
+  static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4, THREADS = 256;
+};
+template <bool SMALL>
+struct Cfg<double, SMALL> {
   static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4, THREADS = 256;
 };
 
@@ -79,12 +88,13 @@ struct Cfg<double> {
 // 2 upper (syrk): tiles strictly outside the triangle are not launched and
 // elements outside it are left untouched.  mode & 4: C = alpha * acc without
 // reading C (trmm overwrites its operand).
-template <typename T, class OA, class OB>
-__global__ void __launch_bounds__(Cfg<T>::THREADS)
+template <typename T, class OA, class OB, bool SMALL>
+__global__ void __launch_bounds__(Cfg<T, SMALL>::THREADS)
     gemm_kernel(long m, long n, long k, T alpha, OA opA, OB opB, T beta, T *C, long ldc, int mode) {
+  using CF = Cfg<T, SMALL>;
   const int tri = mode & 3;
-  constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN, BK = Cfg<T>::BK, TM = Cfg<T>::TM, TN = Cfg<T>::TN;
-  constexpr int NT = Cfg<T>::THREADS;
+  constexpr int BM = CF::BM, BN = CF::BN, BK = CF::BK, TM = CF::TM, TN = CF::TN;
+  constexpr int NT = CF::THREADS;
   constexpr int LA = BM * BK / NT, LB = BN * BK / NT;  // loads per thread per tile
   constexpr int TX = BN / TN;                           // threads along n
   __shared__ T As[2][BK][BM + 4];
@@ -197,20 +207,30 @@ __global__ void __launch_bounds__(Cfg<T>::THREADS)
   }
 }
 
-template <typename T, class OA, class OB>
-static void launch(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int mode) {
-  constexpr int BM = Cfg<T>::BM, BN = Cfg<T>::BN;
-  if (m <= 0 || n <= 0) return;
+template <typename T, bool SMALL, class OA, class OB>
+static void launch_cfg(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int mode) {
+  using CF = Cfg<T, SMALL>;
   dim3 grid;
   if ((mode & 3) == 0) {
-    grid = dim3(unsigned(ceil_div(n, BN)), unsigned(ceil_div(m, BM)));
+    grid = dim3(unsigned(ceil_div(n, CF::BN)), unsigned(ceil_div(m, CF::BM)));
   } else {
-    const long nt = ceil_div(n, BM);  // BM == BN for every configuration
+    const long nt = ceil_div(n, CF::BM);  // BM == BN for every configuration
     grid = dim3(unsigned(nt * (nt + 1) / 2));
   }
-  gemm_kernel<T, OA, OB><<<grid, Cfg<T>::THREADS, 0, ctx().stream>>>(m, n, k, alpha, a, b, beta, C, ldc, mode);
+  gemm_kernel<T, OA, OB, SMALL><<<grid, CF::THREADS, 0, ctx().stream>>>(m, n, k, alpha, a, b, beta, C, ldc, mode);
   EXB_LAUNCH("gemm kernel");
   count_launch();
+}
+
+template <typename T, class OA, class OB>
+static void launch(long m, long n, long k, T alpha, OA a, OB b, T beta, T *C, long ldc, int mode) {
+  if (m <= 0 || n <= 0) return;
+  constexpr int BM = Cfg<T, false>::BM;
+  const long tiles = (mode & 3) == 0 ? ceil_div(m, BM) * ceil_div(n, BM) : ceil_div(n, BM) * (ceil_div(n, BM) + 1) / 2;
+  if (std::is_same<T, float>::value && tiles < ctx().sm_count)
+    launch_cfg<T, true>(m, n, k, alpha, a, b, beta, C, ldc, mode);
+  else
+    launch_cfg<T, false>(m, n, k, alpha, a, b, beta, C, ldc, mode);
 }
 
 // src/level3/gemm.py:17-47 with the wrapper's beta pre-pass fused

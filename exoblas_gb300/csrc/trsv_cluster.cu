@@ -884,8 +884,8 @@ __global__ void __launch_bounds__(kNTS, 1) trsv_cluster_kernel(Args<T> a) {
 // launch can then finish all the work by itself, so the extra CTAs only
 // speed it up and can never hold an SM that a cluster still needs: a CTA
 // that finds the clusters incomplete waits at most kExtraWaitNs and leaves.
-// Their shared memory is as large as a clustered CTA's, so none of them
-// shares an SM with a solver CTA.
+// Two of them fit on a free SM; a clustered CTA takes more shared memory
+// than is left next to one, so none of them shares an SM with a solver CTA.
 constexpr unsigned long long kExtraWaitNs = 20000;
 template <typename T>
 __global__ void __launch_bounds__(kNT, 1) trsv_extra_stream_kernel(Args<T> a) {
@@ -1024,9 +1024,10 @@ size_t trsv_cluster_smem() {
   const size_t a = CS == tc::kCS2 ? sizeof(tc::SmemSolver2<T>) : sizeof(tc::SmemSolver<T, CS>);
   const size_t b = sizeof(tc::SmemStream<T>);
   size_t s = a > b ? a : b;
-  // more than half an SM's shared memory, so a solver CTA never shares its
-  // SM (and FP64 pipe) with a streaming CTA
-  return s > size_t(116) * 1024 ? s : size_t(116) * 1024;
+  // more than half an SM's shared memory, and more than what is left next to
+  // an extra streaming CTA, so a solver CTA never shares its SM (and FP64
+  // pipe) with a streaming CTA of either launch
+  return s > size_t(130) * 1024 ? s : size_t(130) * 1024;
 }
 
 template <typename T, int CS>
@@ -1125,8 +1126,20 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
   EXB_CUDA(cudaMemsetAsync(a.xflag, 0, flag_b, c.stream));
   trsv_inverse_kernel<T><<<nb, kNT, 0, c.stream>>>(a);
   EXB_LAUNCH("trsv inverse kernel");
-  // SMs the clustered launch leaves free, when it is at its size limit
-  const long extra = clusters == maxc ? long(c.sm_count) - clusters * CS : 0;
+  // SMs the clustered launch leaves free, when it is at its size limit, times
+  // the extra CTAs that fit on one of them (two: one computes while the other
+  // waits on memory)
+  const long free_sms = clusters == maxc ? long(c.sm_count) - clusters * CS : 0;
+  long extra = 0;
+  if (free_sms > 0) {
+    const size_t esmem = sizeof(SmemStream<T>);
+    static std::once_flag attr_set[64];
+    std::call_once(attr_set[dev], [&] {
+      EXB_CUDA(cudaFuncSetAttribute(trsv_extra_stream_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    int(esmem)));
+    });
+    extra = free_sms * resident_per_sm(reinterpret_cast<const void *>(trsv_extra_stream_kernel<T>), kNT, esmem);
+  }
   const bool use_extra = extra > 0 && chunk_items(nb) > 0;
   if (use_extra) {
     if (!c.side) {
@@ -1144,13 +1157,7 @@ bool trsv_cluster(bool upper, bool trans, bool unit, long n, const T *A, long ld
     EXB_CUDA(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T, 8>, a));
   count_launch(2);
   if (use_extra) {
-    const size_t smem = CS == 16 ? trsv_cluster_smem<T, 16>() : trsv_cluster_smem<T, 8>();
-    static std::once_flag attr_set[64];
-    std::call_once(attr_set[dev], [&] {
-      EXB_CUDA(cudaFuncSetAttribute(trsv_extra_stream_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    int(smem)));
-    });
-    trsv_extra_stream_kernel<T><<<unsigned(extra), kNT, smem, c.side>>>(a);
+    trsv_extra_stream_kernel<T><<<unsigned(extra), kNT, sizeof(SmemStream<T>), c.side>>>(a);
     EXB_LAUNCH("trsv extra streaming kernel");
     count_launch();
     EXB_CUDA(cudaEventRecord(c.join, c.side));
