@@ -1047,7 +1047,8 @@ def run_serve(args):
     args.per_call_sample requests of the same stream, one call after another
     on one stream (blocking calls, as a CPU BLAS user makes them): plain
     per-call launches with the native FFMA / DFMA kernels, and per-call with
-    the same precision paths as the server."""
+    the same precision paths as the server.  The speedups compare those with
+    the server replaying the same sample (same requests, same offsets)."""
     import torch
 
     import exoblas_gb300 as eb
@@ -1081,6 +1082,7 @@ def run_serve(args):
     srv.drain()
     clk = clocks.stop()
     st = srv.stats()
+    bst = srv.batch_stats()
     srv.close()
     span = st["completed"] / st["solves_per_s"] if st["solves_per_s"] > 0 else float("nan")
     flops = sum(w[0] for w in work)
@@ -1135,6 +1137,13 @@ def run_serve(args):
 
     base = per_call(False)
     same = per_call(True)
+    # the server on exactly the per-call sample (same requests, same arrival
+    # offsets), so the ratios below compare one request set
+    srv = serve.Server(workers=W, hbm_budget=W * reserve, scratch_reserve=reserve)
+    srv.replay(sample, offsets[:len(sample)])
+    srv.drain()
+    st_s = srv.stats()
+    srv.close()
     err = serve_errors(torch, eb, call, stream, built)
     line = {
         "metric": METRIC, "unit": "solves/s", "value": round(st["solves_per_s"], 1), "higher_is_better": True,
@@ -1149,8 +1158,12 @@ def run_serve(args):
         "effective_tflops": round(flops / span / 1e12, 2) if span == span else None,
         "per_call_native": dict(base, sample=len(sample)),
         "per_call_same_paths": dict(same, sample=len(sample)),
-        "speedup_vs_per_call": round(st["solves_per_s"] / base["solves_per_s"], 2),
-        "speedup_vs_per_call_same_paths": round(st["solves_per_s"] / same["solves_per_s"], 2),
+        "device_batches": {"requests": bst["batched"], "batches": bst["batches"],
+                           "requests_per_batch": round(bst["per_batch"], 1)},
+        "server_on_sample": {"solves_per_s": round(st_s["solves_per_s"], 1), "p50_ms": round(st_s["p50_s"] * 1e3, 3),
+                             "p99_ms": round(st_s["p99_s"] * 1e3, 3), "sample": len(sample)},
+        "speedup_vs_per_call": round(st_s["solves_per_s"] / base["solves_per_s"], 2),
+        "speedup_vs_per_call_same_paths": round(st_s["solves_per_s"] / same["solves_per_s"], 2),
         "error": err, "clocks": clk,
     }
     print(json.dumps(line))

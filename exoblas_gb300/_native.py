@@ -122,6 +122,7 @@ EXTRA = {
     "exoblas_server_replay": ("i", "pppzp"),
     "exoblas_server_drain": ("i", "p"),
     "exoblas_server_stats": ("i", "pp"),
+    "exoblas_server_batch_stats": ("i", "pp"),
     "exoblas_server_destroy": ("i", "p"),
     "exoblas_reserve_scratch": ("i", "z"),
 }

@@ -27,6 +27,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.h"
 #include "common.cuh"
 #include "runtime.h"
 
@@ -35,7 +36,13 @@ namespace bt {
 
 constexpr int kThreads = 256;
 
-enum UnitKind : int { kGemmTile = 0, kGemvRows = 1, kGemvCols = 2, kTrsv = 3 };
+// Unit kinds.  The batch API's calls use the first four (sgemm tiles, dgemv
+// rows / columns, strsv); the request server's device batches also use the
+// other precision of each (dgemm / dsyrk tiles, sgemv, dtrsv).
+enum UnitKind : int {
+  kGemmTile = 0, kGemvRows = 1, kGemvCols = 2, kTrsv = 3,
+  kDGemmTile = 4, kSGemvRows = 5, kSGemvCols = 6, kDTrsv = 7
+};
 
 struct Unit {
   int kind;
@@ -44,49 +51,38 @@ struct Unit {
   int cfg;     // gemm tile config
 };
 
-struct Op {  // device copy of exoblas_batch_op, normalised
-  int op;
-  int f0, f1, f2;
-  int m, n, k;
-  double alpha, beta;
-  const void *A;
-  long lda;
-  const void *B;
-  long ldb;
-  void *C;
-  long ldc;
-};
 
 // ------------------------------------------------------------ gemm tiles --
 // One TM x TN tile of C = alpha op(A) op(B) + beta C: RM x RN outputs per
 // thread, 16-deep K slices double-buffered in shared memory with the next
 // slice prefetched into registers while the current one is multiplied.
-template <int TM, int TN, int RM, int RN>
-__device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
+template <typename T, int TM, int TN, int RM, int RN>
+__device__ void gemm_tile(const Op &o, int m0, int n0, void *smv) {
   constexpr int BK = 16;
   constexpr int TX = TN / RN, TY = TM / RM;
   constexpr int LA = BK * TM / kThreads, LB = BK * TN / kThreads;
   static_assert(TX * TY == kThreads, "tile shape");
-  float *As = sm, *Bs = sm + 2 * BK * TM;  // [2][BK][TM], [2][BK][TN]
-  const float *A = static_cast<const float *>(o.A), *B = static_cast<const float *>(o.B);
-  float *C = static_cast<float *>(o.C);
+  T *sm = static_cast<T *>(smv);
+  T *As = sm, *Bs = sm + 2 * BK * TM;  // [2][BK][TM], [2][BK][TN]
+  const T *A = static_cast<const T *>(o.A), *B = static_cast<const T *>(o.B);
+  T *C = static_cast<T *>(o.C);
   const bool ta = o.f0 != 111, tb = o.f1 != 111;
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-  float ra[LA], rb[LB];
+  T ra[LA], rb[LB];
   auto fetch = [&](int k0) {
 #pragma unroll
     for (int s = 0; s < LA; ++s) {
       const int e = threadIdx.x + s * kThreads;
       const int kk = ta ? e / TM : e % BK, i = ta ? e % TM : e / BK;
       const long gi = m0 + i, gk = k0 + kk;
-      ra[s] = (gi < o.m && gk < o.k) ? (ta ? A[gk * o.lda + gi] : A[gi * o.lda + gk]) : 0.f;
+      ra[s] = (gi < o.m && gk < o.k) ? (ta ? A[gk * o.lda + gi] : A[gi * o.lda + gk]) : T(0);
     }
 #pragma unroll
     for (int s = 0; s < LB; ++s) {
       const int e = threadIdx.x + s * kThreads;
       const int kk = tb ? e % BK : e / TN, j = tb ? e / BK : e % TN;
       const long gj = n0 + j, gk = k0 + kk;
-      rb[s] = (gj < o.n && gk < o.k) ? (tb ? B[gj * o.ldb + gk] : B[gk * o.ldb + gj]) : 0.f;
+      rb[s] = (gj < o.n && gk < o.k) ? (tb ? B[gj * o.ldb + gk] : B[gk * o.ldb + gj]) : T(0);
     }
   };
   auto stash = [&](int buf) {
@@ -103,11 +99,11 @@ __device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
       Bs[(buf * BK + kk) * TN + j] = rb[s];
     }
   };
-  float acc[RM][RN];
+  T acc[RM][RN];
 #pragma unroll
   for (int i = 0; i < RM; ++i)
 #pragma unroll
-    for (int j = 0; j < RN; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < RN; ++j) acc[i][j] = T(0);
   __syncthreads();  // the previous unit may still read shared memory
   fetch(0);
   stash(0);
@@ -118,7 +114,7 @@ __device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
     if (more) fetch(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      float a[RM], b[RN];
+      T a[RM], b[RN];
 #pragma unroll
       for (int i = 0; i < RM; ++i) a[i] = As[(buf * BK + kk) * TM + ty * RM + i];
 #pragma unroll
@@ -126,13 +122,13 @@ __device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
 #pragma unroll
       for (int i = 0; i < RM; ++i)
 #pragma unroll
-        for (int j = 0; j < RN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < RN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
     }
     if (more) stash(buf ^ 1);
     buf ^= 1;
     __syncthreads();
   }
-  const float alpha = float(o.alpha), beta = float(o.beta);
+  const T alpha = T(o.alpha), beta = T(o.beta);
 #pragma unroll
   for (int i = 0; i < RM; ++i) {
     const long gi = m0 + ty * RM + i;
@@ -141,7 +137,8 @@ __device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
     for (int j = 0; j < RN; ++j) {
       const long gj = n0 + tx + j * TX;
       if (gj >= o.n) continue;
-      float *c = C + gi * o.ldc + gj;
+      if ((o.tri == 1 && gj > gi) || (o.tri == 2 && gj < gi)) continue;  // outside syrk's triangle
+      T *c = C + gi * o.ldc + gj;
       *c = alpha * acc[i][j] + beta * *c;
     }
   }
@@ -149,28 +146,29 @@ __device__ void gemm_tile(const Op &o, int m0, int n0, float *sm) {
 
 // -------------------------------------------------------------- gemv -------
 // NoTrans: rows [r0, r0+128) of y = beta y + alpha A x, a warp per row.
+template <typename T>
 __device__ void gemv_rows(const Op &o, int r0) {
-  const double *A = static_cast<const double *>(o.A), *x = static_cast<const double *>(o.B);
-  double *y = static_cast<double *>(o.C);
+  const T *A = static_cast<const T *>(o.A), *x = static_cast<const T *>(o.B);
+  T *y = static_cast<T *>(o.C);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long incx = o.ldb, incy = o.ldc;
-  const double *xb = incx < 0 ? x + (1 - long(o.n)) * incx : x;
-  double *yb = incy < 0 ? y + (1 - long(o.m)) * incy : y;
+  const T *xb = incx < 0 ? x + (1 - long(o.n)) * incx : x;
+  T *yb = incy < 0 ? y + (1 - long(o.m)) * incy : y;
   for (int r = r0 + warp; r < r0 + 128 && r < o.m; r += kThreads / 32) {
-    const double *a = A + long(r) * o.lda;
-    double s0 = 0, s1 = 0;
+    const T *a = A + long(r) * o.lda;
+    T s0 = 0, s1 = 0;
     int j = lane;
     for (; j + 32 < o.n; j += 64) {
       s0 = fma(a[j], xb[j * incx], s0);
       s1 = fma(a[j + 32], xb[(j + 32) * incx], s1);
     }
     if (j < o.n) s0 = fma(a[j], xb[j * incx], s0);
-    double s = s0 + s1;
+    T s = s0 + s1;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if (lane == 0) {
-      double *yr = yb + long(r) * incy;
-      *yr = o.alpha * s + o.beta * *yr;
+      T *yr = yb + long(r) * incy;
+      *yr = T(o.alpha) * s + T(o.beta) * *yr;
     }
   }
 }
@@ -178,22 +176,23 @@ __device__ void gemv_rows(const Op &o, int r0) {
 // y has n entries).  Lane quad q = tid / 4 owns column c0 + q; its four
 // lanes take rows i = 4t + (tid % 4) and combine with two shuffles in a
 // fixed order, so no shared memory or block barrier is involved.
+template <typename T>
 __device__ void gemv_cols(const Op &o, int c0) {
-  const double *A = static_cast<const double *>(o.A), *x = static_cast<const double *>(o.B);
-  double *y = static_cast<double *>(o.C);
+  const T *A = static_cast<const T *>(o.A), *x = static_cast<const T *>(o.B);
+  T *y = static_cast<T *>(o.C);
   const long incx = o.ldb, incy = o.ldc;
-  const double *xb = incx < 0 ? x + (1 - long(o.m)) * incx : x;
-  double *yb = incy < 0 ? y + (1 - long(o.n)) * incy : y;
+  const T *xb = incx < 0 ? x + (1 - long(o.m)) * incx : x;
+  T *yb = incy < 0 ? y + (1 - long(o.n)) * incy : y;
   const int col = threadIdx.x >> 2, grp = threadIdx.x & 3;
   const long j = c0 + col;
-  double s = 0;
+  T s = 0;
   if (j < o.n)
     for (int i = grp; i < o.m; i += 4) s = fma(A[long(i) * o.lda + j], xb[i * incx], s);
   s += __shfl_xor_sync(0xffffffffu, s, 1);
   s += __shfl_xor_sync(0xffffffffu, s, 2);
   if (grp == 0 && j < o.n) {
-    double *yj = yb + j * incy;
-    *yj = o.alpha * s + o.beta * *yj;
+    T *yj = yb + j * incy;
+    *yj = T(o.alpha) * s + T(o.beta) * *yj;
   }
 }
 
@@ -202,40 +201,41 @@ __device__ void gemv_cols(const Op &o, int c0) {
 // block's right-hand side with the solved prefix (row dots), then warp 0
 // substitutes through the 32 x 32 diagonal block with shuffles.  Effective
 // lower formulation as in trsv.cu.
-__device__ void trsv_cta(const Op &o, float *sm) {
-  const float *A = static_cast<const float *>(o.A);
-  float *x = static_cast<float *>(o.C);
+template <typename T>
+__device__ void trsv_cta(const Op &o, void *smv) {
+  const T *A = static_cast<const T *>(o.A);
+  T *x = static_cast<T *>(o.C);
   const long n = o.m, lda = o.lda, inc = o.ldc;
-  float *xb = inc < 0 ? x + (1 - n) * inc : x;
+  T *xb = inc < 0 ? x + (1 - n) * inc : x;
   const bool upper = o.f0 == 121, trans = o.f1 != 111, unit = o.f2 != 131;
   const bool rev = upper != trans;
   auto cidx = [&](long k) { return rev ? n - 1 - k : k; };
-  auto L = [&](long i, long j) -> float {
+  auto L = [&](long i, long j) -> T {
     const long ci = cidx(i), cj = cidx(j);
     return trans ? A[cj * lda + ci] : A[ci * lda + cj];
   };
-  float *z = sm;  // solved values in effective order (n <= 4096)
+  T *z = static_cast<T *>(smv);  // solved values in effective order (n <= 4096)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (long b0 = 0; b0 < n; b0 += 32) {
     const long rows = n - b0 < 32 ? n - b0 : 32;
     // rhs for the block: b - L[b0.., 0:b0] z[0:b0], four rows per warp
     for (int r = warp; r < rows; r += kThreads / 32) {
       const long i = b0 + r;
-      float s = 0.f;
-      for (long j = lane; j < b0; j += 32) s = fmaf(L(i, j), z[j], s);
+      T s = T(0);
+      for (long j = lane; j < b0; j += 32) s = fma(L(i, j), z[j], s);
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
       if (lane == 0) z[i] = xb[cidx(i) * inc] - s;
     }
     __syncthreads();
     if (warp == 0) {
-      float v = lane < rows ? z[b0 + lane] : 0.f;
+      T v = lane < rows ? z[b0 + lane] : T(0);
       for (int j = 0; j < rows; ++j) {
-        float xj = v;
+        T xj = v;
         if (lane == j && !unit) xj = v / L(b0 + j, b0 + j);
         xj = __shfl_sync(0xffffffffu, xj, j);
         if (lane == j) v = xj;
-        if (lane > j && lane < rows) v = fmaf(-L(b0 + lane, b0 + j), xj, v);
+        if (lane > j && lane < rows) v = fma(-L(b0 + lane, b0 + j), xj, v);
       }
       if (lane < rows) z[b0 + lane] = v;
     }
@@ -260,20 +260,32 @@ __global__ void __launch_bounds__(kThreads)
     switch (un.kind) {
       case kGemmTile:
         if (un.cfg == 0)
-          gemm_tile<32, 32, 2, 2>(o, un.r0, un.c0, smem_f);
+          gemm_tile<float, 32, 32, 2, 2>(o, un.r0, un.c0, smem_f);
         else if (un.cfg == 1)
-          gemm_tile<64, 64, 4, 4>(o, un.r0, un.c0, smem_f);
+          gemm_tile<float, 64, 64, 4, 4>(o, un.r0, un.c0, smem_f);
         else
-          gemm_tile<128, 128, 8, 8>(o, un.r0, un.c0, smem_f);
+          gemm_tile<float, 128, 128, 8, 8>(o, un.r0, un.c0, smem_f);
+        break;
+      case kDGemmTile:  // 64 x 64: the FP64 operand slices fill the same shared memory
+        gemm_tile<double, 64, 64, 4, 4>(o, un.r0, un.c0, smem_f);
         break;
       case kGemvRows:
-        gemv_rows(o, un.r0);
+        gemv_rows<double>(o, un.r0);
         break;
       case kGemvCols:
-        gemv_cols(o, un.c0);
+        gemv_cols<double>(o, un.c0);
+        break;
+      case kSGemvRows:
+        gemv_rows<float>(o, un.r0);
+        break;
+      case kSGemvCols:
+        gemv_cols<float>(o, un.c0);
+        break;
+      case kDTrsv:
+        trsv_cta<double>(o, smem_f);
         break;
       default:
-        trsv_cta(o, smem_f);
+        trsv_cta<float>(o, smem_f);
         break;
     }
   }
@@ -503,6 +515,132 @@ static double unit_cost(const exoblas_batch_op &b, int kind, int cfg) {
   }
 }
 
+// Work units of one call, appended to `us` with their estimated cost.
+// Returns false for an op code it does not know.
+static bool add_units(const Op &o, int idx, std::vector<std::pair<double, Unit>> &us, double &flops, double &bytes) {
+  exoblas_batch_op b{};  // cost model view
+  b.m = o.m;
+  b.n = o.n;
+  b.k = o.k;
+  auto tiles = [&](int kind, int cfg, int TM, int TN) {
+    for (int r = 0; r < o.m; r += TM)
+      for (int cc = 0; cc < o.n; cc += TN) {
+        if (o.tri == 1 && cc > r + TM - 1) continue;  // tile entirely above the lower triangle
+        if (o.tri == 2 && cc + TN - 1 < r) continue;  // entirely below the upper triangle
+        us.push_back({unit_cost(b, kGemmTile, cfg), Unit{kind, idx, r, cc, cfg}});
+      }
+  };
+  switch (o.op) {
+    case EXOBLAS_BATCH_SGEMM:
+    case kOpSSyrk: {
+      if (o.m == 0 || o.n == 0) break;
+      const int cf = tile_config(o.m, o.n, o.k);
+      tiles(kGemmTile, cf, kTiles[cf][0], kTiles[cf][1]);
+      flops += 2.0 * o.m * o.n * o.k;
+      break;
+    }
+    case kOpDGemm:
+    case kOpDSyrk:
+      if (o.m == 0 || o.n == 0) break;
+      tiles(kDGemmTile, 1, 64, 64);
+      flops += 2.0 * o.m * o.n * o.k;
+      break;
+    case EXOBLAS_BATCH_DGEMV:
+    case kOpSGemv: {
+      if (o.m == 0 || o.n == 0) break;
+      const bool dbl = o.op == EXOBLAS_BATCH_DGEMV;
+      if (o.f0 == 111) {
+        for (int r = 0; r < o.m; r += 128)
+          us.push_back({unit_cost(b, kGemvRows, 0), Unit{dbl ? kGemvRows : kSGemvRows, idx, r, 0, 0}});
+      } else {
+        for (int cc = 0; cc < o.n; cc += 64)
+          us.push_back({unit_cost(b, kGemvCols, 0), Unit{dbl ? kGemvCols : kSGemvCols, idx, 0, cc, 0}});
+      }
+      bytes += (double(o.m) * o.n + o.m + 2.0 * o.n) * (dbl ? 8 : 4);
+      break;
+    }
+    case EXOBLAS_BATCH_STRSV:
+    case kOpDTrsv: {
+      if (o.m == 0) break;
+      const bool dbl = o.op == kOpDTrsv;
+      us.push_back({unit_cost(b, kTrsv, 0) * (dbl ? 8 : 1), Unit{dbl ? kDTrsv : kTrsv, idx, 0, 0, 0}});
+      bytes += (double(o.m) * (o.m + 1) / 2 + 2.0 * o.m) * (dbl ? 8 : 4);
+      break;
+    }
+    default:
+      return false;
+  }
+  return true;
+}
+
+// One device batch at a time on the runner's own stream: the request
+// server's continuous batching of small requests.
+struct TickRunner {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Op *dops = nullptr;
+  Unit *dunits = nullptr;
+  int *ticket = nullptr;
+  size_t cap_ops = 0, cap_units = 0;
+  void *pinned = nullptr;
+  size_t cap_pinned = 0;
+};
+
+TickRunner *tick_create() {
+  TickRunner *t = new TickRunner();
+  EXB_CUDA(cudaGetDevice(&t->device));
+  EXB_CUDA(cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking));
+  EXB_CUDA(cudaMalloc(&t->ticket, 256));
+  return t;
+}
+
+void tick_destroy(TickRunner *t) {
+  if (!t) return;
+  cudaStreamSynchronize(t->stream);
+  cudaFree(t->dops);
+  cudaFree(t->dunits);
+  cudaFree(t->ticket);
+  cudaFreeHost(t->pinned);
+  cudaStreamDestroy(t->stream);
+  cudaGetLastError();
+  delete t;
+}
+
+bool tick_run(TickRunner *t, const std::vector<Op> &ops, int sm_count) {
+  std::vector<std::pair<double, Unit>> us;
+  double flops = 0, bytes = 0;
+  for (size_t i = 0; i < ops.size(); ++i)
+    if (!add_units(ops[i], int(i), us, flops, bytes)) return false;
+  if (us.empty()) return true;
+  std::stable_sort(us.begin(), us.end(), [](const std::pair<double, Unit> &a, const std::pair<double, Unit> &b) {
+    return a.first > b.first;
+  });
+  auto grow = [](void **p, size_t &cap, size_t need) {
+    if (need <= cap) return;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    cap = need + need / 2;
+    EXB_CUDA(cudaMalloc(p, cap));
+  };
+  const size_t ob = sizeof(Op) * ops.size(), ub = sizeof(Unit) * us.size();
+  grow(reinterpret_cast<void **>(&t->dops), t->cap_ops, ob);
+  grow(reinterpret_cast<void **>(&t->dunits), t->cap_units, ub);
+  if (ob + ub > t->cap_pinned) {
+    if (t->pinned) EXB_CUDA(cudaFreeHost(t->pinned));
+    t->cap_pinned = (ob + ub) * 2;
+    EXB_CUDA(cudaHostAlloc(&t->pinned, t->cap_pinned, cudaHostAllocDefault));
+  }
+  char *h = static_cast<char *>(t->pinned);
+  memcpy(h, ops.data(), ob);
+  Unit *hu = reinterpret_cast<Unit *>(h + ob);
+  for (size_t i = 0; i < us.size(); ++i) hu[i] = us[i].second;
+  EXB_CUDA(cudaMemcpyAsync(t->dops, h, ob, cudaMemcpyHostToDevice, t->stream));
+  EXB_CUDA(cudaMemcpyAsync(t->dunits, hu, ub, cudaMemcpyHostToDevice, t->stream));
+  launch_units(t->dops, t->dunits, int(us.size()), t->ticket, t->stream, sm_count);
+  EXB_CUDA(cudaStreamSynchronize(t->stream));
+  return true;
+}
+
 }  // namespace bt
 }  // namespace exb
 
@@ -549,40 +687,20 @@ int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_ba
       for (const void *p : {b.A, b.B, static_cast<const void *>(b.C)})
         if (p && !is_device_pointer(p)) fail(EXOBLAS_INVALID_VALUE, "batch operands must be device pointers");
       switch (b.op) {
-        case EXOBLAS_BATCH_SGEMM: {
-          if (b.m == 0 || b.n == 0) break;
-          const int cf = bt::tile_config(b.m, b.n, b.k);
-          const int TM = bt::kTiles[cf][0], TN = bt::kTiles[cf][1];
-          for (int r = 0; r < b.m; r += TM)
-            for (int cc = 0; cc < b.n; cc += TN)
-              us.push_back({bt::unit_cost(b, bt::kGemmTile, cf), bt::Unit{bt::kGemmTile, i, r, cc, cf}});
-          flops += 2.0 * b.m * b.n * b.k;
+        case EXOBLAS_BATCH_SGEMM:
           break;
-        }
-        case EXOBLAS_BATCH_DGEMV: {
-          if (b.m == 0 || b.n == 0) break;
-          if (b.ldb == 0 || b.ldc == 0) fail(EXOBLAS_INVALID_VALUE, "zero vector stride in a batch dgemv");
-          if (b.flags[0] == 111) {
-            for (int r = 0; r < b.m; r += 128)
-              us.push_back({bt::unit_cost(b, bt::kGemvRows, 0), bt::Unit{bt::kGemvRows, i, r, 0, 0}});
-          } else {
-            for (int cc = 0; cc < b.n; cc += 64)
-              us.push_back({bt::unit_cost(b, bt::kGemvCols, 0), bt::Unit{bt::kGemvCols, i, 0, cc, 0}});
-          }
-          bytes += (double(b.m) * b.n + b.m + 2.0 * b.n) * 8;
+        case EXOBLAS_BATCH_DGEMV:
+          if (b.m != 0 && b.n != 0 && (b.ldb == 0 || b.ldc == 0))
+            fail(EXOBLAS_INVALID_VALUE, "zero vector stride in a batch dgemv");
           break;
-        }
-        case EXOBLAS_BATCH_STRSV: {
-          if (b.m == 0) break;
+        case EXOBLAS_BATCH_STRSV:
           if (b.m > 4096) fail(EXOBLAS_INVALID_VALUE, "batch strsv supports N <= 4096");
-          if (b.ldc == 0) fail(EXOBLAS_INVALID_VALUE, "zero stride in a batch strsv");
-          us.push_back({bt::unit_cost(b, bt::kTrsv, 0), bt::Unit{bt::kTrsv, i, 0, 0, 0}});
-          bytes += (double(b.m) * (b.m + 1) / 2 + 2.0 * b.m) * 4;
+          if (b.m != 0 && b.ldc == 0) fail(EXOBLAS_INVALID_VALUE, "zero stride in a batch strsv");
           break;
-        }
         default:
           fail(EXOBLAS_INVALID_VALUE, "unknown batch op");
       }
+      bt::add_units(o, i, us, flops, bytes);
     }
     // longest first; ties keep submission order (stable)
     std::stable_sort(us.begin(), us.end(),

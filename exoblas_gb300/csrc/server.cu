@@ -1,18 +1,28 @@
 // Request server with continuous batching over the exo_* entry points.
 //
 // Requests (gemm / gemv / trsv / syrk in single or double precision, every
-// operand resident in device memory) are submitted as they arrive.  Each of
-// W worker threads owns one CUDA stream and its own workspace (the
-// library's per-thread context), pre-grown at start so no worker ever frees
-// device memory while others run.  A request is admitted when a worker slot
-// is free AND its estimated device-memory footprint fits in the admission
-// budget together with everything in flight; admitted requests from
-// different workers run concurrently on the device.  Requests that arrive
-// while others are executing wait in a bounded queue (arrivals beyond its
-// capacity are rejected and counted, so overload degrades gracefully).
-// Single-precision gemm / syrk run the split-BF16 tensor-core path,
-// double-precision gemm / syrk the Ozaki path; gemv and trsv their native
-// kernels.
+// operand resident in device memory) are submitted as they arrive, and take
+// one of two paths by size:
+//  * small requests (gemm / syrk with m n k <= 2^24, gemv with m n <= 2^22,
+//    trsv with n <= 512) go to a batcher thread.  Every tick it takes all
+//    small requests that arrived since the previous tick and runs them as
+//    one device batch (batch.cu: one launch whose CTAs claim the requests'
+//    tiles, row blocks and solves from a ticket) on its own stream; requests
+//    arriving meanwhile join the next tick.  gemm / syrk run FFMA / DFMA
+//    tiles there.
+//  * larger requests go to W worker threads, each owning one CUDA stream and
+//    its own workspace (the library's per-thread context), pre-grown at
+//    start so no worker ever frees device memory while others run.  A
+//    request is admitted when a worker slot is free AND its estimated
+//    device-memory footprint fits in the admission budget together with
+//    everything in flight.  Single-precision gemm / syrk run the split-BF16
+//    tensor-core path, double-precision gemm / syrk the Ozaki path; gemv and
+//    trsv their native kernels.
+// Device batches and worker requests run concurrently on the device.
+// Requests that arrive while others are executing wait in bounded queues
+// (arrivals beyond capacity are rejected and counted, so overload degrades
+// gracefully).  Every path is deterministic and the path depends on the
+// request's size only, so a request gives the same bits alone and in a mix.
 // Latency = completion - arrival, measured on the host clock.
 #include <cuda_runtime.h>
 
@@ -25,6 +35,7 @@
 #include <thread>
 #include <vector>
 
+#include "batch.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "runtime.h"
@@ -62,9 +73,123 @@ static size_t footprint(const exoblas_request &r) {
   }
 }
 
+// Requests the device batcher takes (sizes where one batch launch beats a
+// call of its own; larger ones keep the full-device kernels).
+static bool batchable(const exoblas_request &r) {
+  switch (r.op) {
+    case EXOBLAS_REQ_GEMM:
+    case EXOBLAS_REQ_SYRK: {
+      const double n = r.op == EXOBLAS_REQ_SYRK ? r.m : r.n;
+      return double(r.m) * n * r.k <= double(1 << 24);
+    }
+    case EXOBLAS_REQ_GEMV:
+      return double(r.m) * r.n <= double(1 << 22) && r.ldb != 0 && r.ldc != 0;
+    default:
+      return r.m <= 512 && r.ldc != 0;
+  }
+}
+
+// The device-batch description of a request.
+static bt::Op batch_op(const exoblas_request &r) {
+  bt::Op o{};
+  const bool dbl = r.precision == 2;
+  o.m = r.m;
+  o.n = r.n;
+  o.k = r.k;
+  o.alpha = r.alpha;
+  o.beta = r.beta;
+  o.A = r.A;
+  o.lda = r.lda;
+  o.B = r.B;
+  o.ldb = r.ldb;
+  o.C = r.C;
+  o.ldc = r.ldc;
+  switch (r.op) {
+    case EXOBLAS_REQ_GEMM:
+      o.op = dbl ? bt::kOpDGemm : EXOBLAS_BATCH_SGEMM;
+      o.f0 = r.flags[0];
+      o.f1 = r.flags[1];
+      break;
+    case EXOBLAS_REQ_SYRK: {
+      // C_tri = alpha op(A) op(A)^T + beta C_tri: a gemm of op(A) (n x k)
+      // with op(A)^T, on the stored triangle only
+      const bool trans = r.flags[1] != CblasNoTrans;
+      o.op = dbl ? bt::kOpDSyrk : bt::kOpSSyrk;
+      o.n = r.m;
+      o.f0 = trans ? CblasTrans : CblasNoTrans;
+      o.f1 = trans ? CblasNoTrans : CblasTrans;
+      o.B = r.A;
+      o.ldb = r.lda;
+      o.tri = r.flags[0] == CblasUpper ? 2 : 1;
+      break;
+    }
+    case EXOBLAS_REQ_GEMV:
+      o.op = dbl ? EXOBLAS_BATCH_DGEMV : bt::kOpSGemv;
+      o.f0 = r.flags[0];
+      break;
+    default:
+      o.op = dbl ? bt::kOpDTrsv : EXOBLAS_BATCH_STRSV;
+      o.f0 = r.flags[0];
+      o.f1 = r.flags[1];
+      o.f2 = r.flags[2];
+      break;
+  }
+  return o;
+}
+
 struct Server {
   int device = 0;
   int workers = 1;
+  int sm_count = 0;
+  // device batcher: small requests waiting for the next tick
+  std::deque<Item> small;
+  std::condition_variable cv_batch;
+  std::thread batcher;
+  bool batch_busy = false;
+  std::atomic<long> batched{0}, ticks{0};
+
+  void run_batcher() {
+    cudaSetDevice(device);
+    bt::TickRunner *tr = nullptr;
+    try {
+      tr = bt::tick_create();
+    } catch (const Error &) {
+    }
+    for (;;) {
+      std::vector<Item> tick;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_batch.wait(lk, [&] { return stop || !small.empty(); });
+        if (stop && small.empty()) break;
+        tick.assign(small.begin(), small.end());
+        small.clear();
+        batch_busy = true;
+      }
+      std::vector<bt::Op> ops;
+      ops.reserve(tick.size());
+      for (const Item &it : tick) ops.push_back(batch_op(it.r));
+      bool ok = tr != nullptr;
+      if (ok) {
+        try {
+          ok = bt::tick_run(tr, ops, sm_count);
+        } catch (const Error &) {
+          ok = false;
+        }
+      }
+      const double done = now_s();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const Item &it : tick) latencies.push_back(done - it.arrival);
+        last_completion = std::max(last_completion, done);
+        (ok ? completed : failed).fetch_add(long(tick.size()));
+        batched.fetch_add(long(tick.size()));
+        ticks.fetch_add(1);
+        batch_busy = false;
+      }
+      cv_idle.notify_all();
+    }
+    bt::tick_destroy(tr);
+  }
   size_t budget = 0, inflight_bytes = 0, queue_cap = 0;
   std::mutex mu;
   std::condition_variable cv_work, cv_idle;
@@ -186,7 +311,9 @@ int exoblas_server_create(int workers, size_t hbm_budget_bytes, size_t queue_cap
     s->budget = hbm_budget_bytes ? std::min(hbm_budget_bytes, auto_budget) : auto_budget;
     s->queue_cap = queue_capacity ? queue_capacity : ~size_t(0);
     s->scratch_reserve = scratch_reserve_bytes;
+    s->sm_count = c.sm_count;
     for (int w = 0; w < workers; ++w) s->threads.emplace_back([s, w] { s->run_worker(w); });
+    s->batcher = std::thread([s] { s->run_batcher(); });
     *out = reinterpret_cast<exoblas_server>(s);
   });
 }
@@ -197,16 +324,28 @@ int exoblas_server_submit(exoblas_server server, const exoblas_request *req, dou
     auto *s = reinterpret_cast<sv::Server *>(server);
     if (!s || !req) fail(EXOBLAS_INVALID_VALUE, "NULL server or request");
     sv::Item it{*req, arrival_s < 0 ? sv::now_s() : arrival_s, sv::footprint(*req)};
+    const bool small = sv::batchable(*req);
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (s->first_arrival < 0) s->first_arrival = it.arrival;
-      if (s->queue.size() >= s->queue_cap || it.footprint > s->budget) {
-        s->rejected.fetch_add(1);
-        return;
+      if (small) {
+        if (s->small.size() >= s->queue_cap) {
+          s->rejected.fetch_add(1);
+          return;
+        }
+        s->small.push_back(it);
+      } else {
+        if (s->queue.size() >= s->queue_cap || it.footprint > s->budget) {
+          s->rejected.fetch_add(1);
+          return;
+        }
+        s->queue.push_back(it);
       }
-      s->queue.push_back(it);
     }
-    s->cv_work.notify_one();
+    if (small)
+      s->cv_batch.notify_one();
+    else
+      s->cv_work.notify_one();
   });
 }
 
@@ -241,7 +380,7 @@ int exoblas_server_drain(exoblas_server server) {
     auto *s = reinterpret_cast<sv::Server *>(server);
     if (!s) fail(EXOBLAS_INVALID_VALUE, "NULL server");
     std::unique_lock<std::mutex> lk(s->mu);
-    s->cv_idle.wait(lk, [&] { return s->queue.empty() && s->busy == 0; });
+    s->cv_idle.wait(lk, [&] { return s->queue.empty() && s->busy == 0 && s->small.empty() && !s->batch_busy; });
   });
 }
 
@@ -269,6 +408,19 @@ int exoblas_server_stats(exoblas_server server, double *stats) {
   });
 }
 
+// stats[0..2]: requests served by device batches, device batches run, mean
+// requests per batch
+int exoblas_server_batch_stats(exoblas_server server, double *stats) {
+  return guarded("exoblas_server_batch_stats", [&] {
+    auto *s = reinterpret_cast<sv::Server *>(server);
+    if (!s || !stats) fail(EXOBLAS_INVALID_VALUE, "NULL argument");
+    const double b = double(s->batched.load()), t = double(s->ticks.load());
+    stats[0] = b;
+    stats[1] = t;
+    stats[2] = t > 0 ? b / t : 0;
+  });
+}
+
 int exoblas_server_destroy(exoblas_server server) {
   return guarded("exoblas_server_destroy", [&] {
     auto *s = reinterpret_cast<sv::Server *>(server);
@@ -278,7 +430,9 @@ int exoblas_server_destroy(exoblas_server server) {
       s->stop = true;
     }
     s->cv_work.notify_all();
+    s->cv_batch.notify_all();
     for (auto &t : s->threads) t.join();
+    if (s->batcher.joinable()) s->batcher.join();
     delete s;
   });
 }

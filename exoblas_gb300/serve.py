@@ -67,6 +67,12 @@ class Server:
     def drain(self):
         _chk(_native.lib().exoblas_server_drain(self.handle), "exoblas_server_drain")
 
+    def batch_stats(self):
+        """Requests served by device batches, batches run, mean requests per batch."""
+        s = (C.c_double * 3)()
+        _chk(_native.lib().exoblas_server_batch_stats(self.handle, s), "exoblas_server_batch_stats")
+        return {"batched": int(s[0]), "batches": int(s[1]), "per_batch": s[2]}
+
     def stats(self):
         s = (C.c_double * 8)()
         _chk(_native.lib().exoblas_server_stats(self.handle, s), "exoblas_server_stats")

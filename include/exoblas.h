@@ -340,14 +340,18 @@ EXOBLAS_API int exoblas_batch_tile_config(int m, int n, int k);
 
 /* ------------------------------------------------------------- serving --- */
 /* A request server with continuous batching (no counterpart in the
- * reference).  W worker threads, each with its own stream and workspace,
- * take requests as they arrive; a request is admitted when a worker is free
- * and its estimated device-memory footprint fits in the admission budget
- * with everything in flight, so requests arriving while others run start as
- * soon as a slot and memory free up and their work overlaps on the device.
- * Operands are device pointers.  Single-precision gemm / syrk run the
- * split-BF16 path, double gemm / syrk the Ozaki path, gemv / trsv their
- * kernels.
+ * reference).  Small requests (gemm / syrk with m n k <= 2^24, gemv with
+ * m n <= 2^22, trsv with n <= 512) are gathered by a batcher thread: each
+ * tick runs every small request that arrived since the previous tick as one
+ * device batch (one launch over all their tiles, row blocks and solves;
+ * FFMA / DFMA tiles for gemm and syrk), and requests arriving meanwhile join
+ * the next tick.  Larger requests go to W worker threads, each with its own
+ * stream and workspace; such a request is admitted when a worker is free and
+ * its estimated device-memory footprint fits in the admission budget with
+ * everything in flight.  Device batches and worker requests overlap on the
+ * device.  Operands are device pointers.  On the worker path,
+ * single-precision gemm / syrk run the split-BF16 path, double gemm / syrk
+ * the Ozaki path, gemv / trsv their kernels.
  *   GEMM: flags = {TransA, TransB}, m, n, k, A/lda, B/ldb, C/ldc
  *   SYRK: flags = {Uplo, Trans}, m = N, k = K, A/lda, C/ldc
  *   GEMV: flags = {TransA}, m = M, n = N, A/lda, B = X (ldb = incX), C = Y (ldc = incY)
@@ -384,6 +388,9 @@ EXOBLAS_API int exoblas_server_drain(exoblas_server server);
 /* stats[0..7]: completed, rejected, failed, p50 latency s, p99 s, mean s,
  * max s, completed per second (first arrival to last completion) */
 EXOBLAS_API int exoblas_server_stats(exoblas_server server, double *stats);
+/* Continuous batching of small requests: stats[0..2] = requests served by
+ * device batches, device batches run, mean requests per batch. */
+EXOBLAS_API int exoblas_server_batch_stats(exoblas_server server, double *stats);
 EXOBLAS_API int exoblas_server_destroy(exoblas_server server);
 /* grows the calling thread's device workspace to at least `bytes` now */
 EXOBLAS_API int exoblas_reserve_scratch(size_t bytes);

@@ -80,11 +80,15 @@ def _outputs(cases, dev):
 
 
 @pytest.mark.gpu
-def test_served_results_same_alone_and_in_mix(cuda):
+@pytest.mark.parametrize("hi", [400, 1500])
+def test_served_results_same_alone_and_in_mix(cuda, hi):
+    """hi = 400: nearly every request is small enough for the device
+    batches; hi = 1500: the mix straddles the size thresholds, so device
+    batches and worker streams run side by side."""
     from exoblas_gb300 import serve as sv
 
     torch = cuda
-    cases = _cases()
+    cases = _cases(hi=hi)
     # alone: one request at a time, each drained before the next is submitted
     reqs, dev = _requests(torch, cases)
     s = sv.Server(workers=4)
@@ -104,6 +108,8 @@ def test_served_results_same_alone_and_in_mix(cuda):
     st = s.stats()
     assert st["completed"] == len(cases) and st["failed"] == 0
     assert st["p99_s"] >= st["p50_s"] > 0
+    bs = s.batch_stats()
+    assert bs["batched"] > 0 and bs["batches"] >= 1  # small requests went through device batches
     s.close()
     for i, c in enumerate(cases):
         assert alone[i].tobytes() == mixed[i].tobytes(), f"request {i} ({c}) differs alone vs in the mix"
