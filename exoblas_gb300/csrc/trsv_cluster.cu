@@ -20,9 +20,10 @@
 //    helper warps exchange through st.async stores counted on mbarriers.
 //    The operand rows the solver needs are prefetched with cp.async.
 //    A 16-CTA solver CTA also has a publisher warp (x_m to global memory
-//    with its release flag) and a slot-loader warp (sums the streamers'
-//    slots of each block row ahead of time into shared memory), so no
-//    global-memory round trip sits on the helpers' loop.
+//    with its release flag) and two slot-loader warps (even and odd block
+//    rows: sum the streamers' slots of each block row ahead of time into
+//    shared memory), so no global-memory round trip sits on the helpers'
+//    loop.
 //  * every other CTA STREAMS the bulk, tiles L[K, J] with J < K - kD.  Row
 //    K's bulk is split into full chunks of kCT tiles and a tail holding its
 //    newest tiles; each work item writes its 64 partial row sums to its
@@ -57,7 +58,7 @@ namespace tc {
 
 constexpr int kTB = 64;            // block size
 constexpr int kNT = 256;           // threads of a streaming CTA and of the 8-CTA solver
-constexpr int kNTS = 320;          // threads per CTA of a 16-CTA launch: 8 solver warps + publisher + slot loader
+constexpr int kNTS = 352;          // threads per CTA of a 16-CTA launch: 8 solver warps, publisher, 2 slot loaders
 constexpr int kCT = 4;             // tiles per streamer chunk
 static_assert(kCT <= 32, "one ballot bit per tile of an item");
 constexpr int kTailCTAs = 2;       // tail workers per streaming cluster
@@ -520,7 +521,9 @@ constexpr int kCS2 = 16;
 constexpr int kRPC2 = kTB / kCS2;  // 4
 constexpr int kSR = 4;                     // slot-sum ring depth (block rows)
 constexpr int kPubWarp = kNT / 32;         // warp 8
-constexpr int kLoaderWarp = kNT / 32 + 1;  // warp 9
+constexpr int kLoaderWarp = kNT / 32 + 1;  // warps 9, 10: even and odd block rows
+constexpr int kLoaders = 2;
+static_assert(kNTS == 32 * (kLoaderWarp + kLoaders), "16-CTA solver warps");
 constexpr long long kWaitCycles = 4ll << 30;
 
 template <typename T>
@@ -536,7 +539,7 @@ struct SmemSolver2 {
   unsigned long long e2bar[4];
   unsigned long long cready[2];
   int pub_done;    // x_0 .. x_{pub_done-1} published to global memory (publisher -> helpers)
-  int slot_ready;  // slotsum holds block row slot_ready and the rows before it (slot loader -> helpers)
+  int slot_row[kSR];  // slotsum[i] holds block row slot_row[i] (slot loaders -> helpers)
   int slot_used;   // helpers have consumed the slot sums of rows up to slot_used (helpers -> slot loader)
 };
 
@@ -641,7 +644,7 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
     for (int i = 0; i < 2; ++i) arm(sh_u32(&S.e1bar[i]), kXBytes);
     for (int i = 0; i < 4; ++i) arm(sh_u32(&S.e2bar[i]), kXBytes);
     S.pub_done = 0;
-    S.slot_ready = -1;
+    for (int i = 0; i < kSR; ++i) S.slot_row[i] = -1;
     S.slot_used = kD;  // rows 0 .. kD have no bulk part
   }
   cl.sync();  // every barrier of the cluster is initialised before any remote arrive
@@ -769,7 +772,7 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
       }
       T bulk = T(0);
       if (nslots_row(T1) > 0) {
-        wait_count(&S.slot_ready, int(T1), a.status, dead);
+        wait_count(&S.slot_row[T1 % kSR], int(T1), a.status, dead);
         bulk = S.slotsum[T1 % kSR][h];
       }
       S.carry[T1 & 1][h][lane] = (s0 + s1) + (lane == 0 ? bulk : T(0));
@@ -793,11 +796,13 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
       __syncwarp();
       if (lane == 0) st_release_cta(&S.pub_done, int(m + 1));
     }
-  } else if (warp == kLoaderWarp) {
-    // ---------------- slot loader: for block rows in order, wait for the
-    // streamers' slots, sum the owned rows' slots (lane l: row l / 8, slots
-    // l % 8, l % 8 + 8, ... in slot order, then a fixed tree over the eight
-    // lanes of the row) and hand the sums to the helpers through slotsum.
+  } else if (warp < kLoaderWarp + kLoaders) {
+    // ---------------- slot loaders: loader L takes block rows m = kD+1+L,
+    // kD+1+L+kLoaders, ...: waits for the streamers' slots, sums the owned
+    // rows' slots (lane l: row l / 8, slots l % 8 + 8u in slot order, a fixed
+    // tree over u, then a fixed tree over the eight lanes of the row) and
+    // hands the sums to the helpers through slotsum.
+    const int L = warp - kLoaderWarp;
     const int r = lane >> 3, q = lane & 7;
     // one poll of row m's slot flags; true when all are set
     auto flags_ready = [&](long m) -> bool {
@@ -817,35 +822,39 @@ __device__ void solve_chain2(const Args<T> &a, SmemSolver2<T> &S, bool &dead) {
         }
       }
     };
+    // slots c0 + 8u (u = 0..7) of this lane, summed by a fixed tree; the
+    // upper half is empty when the row has at most c0 + 32 slots
+    const T *sl_base = a.slots + R * RPC + r;
+    auto batch = [&](long m, int nc, int c0) -> T {
+      const T *sl = sl_base + (m * a.nch) * kTB;
+      T w[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) w[u] = c0 + q + 8 * u < nc ? __ldcg(sl + long(c0 + q + 8 * u) * kTB) : T(0);
+      const T lo = (w[0] + w[1]) + (w[2] + w[3]);
+      return nc <= c0 + 32 ? lo : lo + ((w[4] + w[5]) + (w[6] + w[7]));
+    };
     bool next_seen = false;
-    for (long m = kD + 1; m < nb; ++m) {
+    for (long m = kD + 1 + L; m < nb; m += kLoaders) {
       const int nc = nslots_row(m);
       wait_count(&S.slot_used, int(m - kSR), a.status, dead);  // row m - kSR consumed
       wait_flags(m, next_seen);
-      // row m's slot loads in flight while row m+1's flags are polled once;
-      // each lane's slots in batches of eight independent loads, added in
-      // slot order
-      T v = T(0);
-      const T *sl = a.slots + (m * a.nch) * kTB + R * RPC + r;
+      // the first batch of loads in flight while the flags of this loader's
+      // next row are polled once
+      const T *sl = sl_base + (m * a.nch) * kTB;
       T w[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) w[u] = q + 8 * u < nc ? __ldcg(sl + long(q + 8 * u) * kTB) : T(0);
-      next_seen = m + 1 < nb && !dead && flags_ready(m + 1);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) v += w[u];
-      for (int c0 = q + 64; c0 < nc; c0 += 64) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) w[u] = c0 + 8 * u < nc ? __ldcg(sl + long(c0 + 8 * u) * kTB) : T(0);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v += w[u];
-      }
+      next_seen = m + kLoaders < nb && !dead && flags_ready(m + kLoaders);
+      T v = (w[0] + w[1]) + (w[2] + w[3]);
+      if (nc > 32) v += (w[4] + w[5]) + (w[6] + w[7]);
+      for (int c0 = 64; c0 < nc; c0 += 64) v += batch(m, nc, c0);
       v += __shfl_xor_sync(0xffffffffu, v, 4);
       v += __shfl_xor_sync(0xffffffffu, v, 2);
       v += __shfl_xor_sync(0xffffffffu, v, 1);
       if (q == 0) S.slotsum[m % kSR][r] = v;
       __syncwarp();
       __threadfence_block();
-      if (lane == 0) st_release_cta(&S.slot_ready, int(m));
+      if (lane == 0) st_release_cta(&S.slot_row[m % kSR], int(m));
     }
   }
   cl.sync();  // no CTA leaves while a peer may still write into its shared memory
@@ -960,13 +969,15 @@ __global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
     }
   }
   __syncthreads();
-  // 32x32 blocks p = 0, 1 at P = 32p:
+  static_assert(kNT == 256 && kTB == 64, "the stages below map 8 warps onto 64x64 blocks");
+  const int w = tid >> 5, lane = tid & 31;
+  // 32x32 blocks p = 0, 1 at P = 32p (lanes 0-15: P = 0, lanes 16-31: P = 32):
   //   W = L[P+16.., P..] inv(A)     W(i, j) = sum_{k=j..15} L[P+16+i][P+k] Y[P+k][P+j]
   {
-    const int P = (tid >> 7) * 32, u = tid & 127, i = u >> 3, jq = u & 7;
+    const int P = (lane >> 4) * 32, i = lane & 15;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int j = h ? 15 - jq : jq;  // column pairs of equal total length
+      const int j = h ? 15 - w : w;
       T s = 0;
       for (int k = j; k < 16; ++k) s = fma(L[P + 16 + i][P + k], Y[P + k][P + j], s);
       L[(P >> 1) + i][32 + j] = s;
@@ -975,10 +986,10 @@ __global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
   __syncthreads();
   //   Y[P+16+i][P+j] = - sum_{k=0..i} Y[P+16+i][P+16+k] W(k, j)
   {
-    const int P = (tid >> 7) * 32, u = tid & 127, ip = u >> 4, j = u & 15;
+    const int P = (lane >> 4) * 32, j = lane & 15;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int i = h ? 15 - ip : ip;  // row pairs of equal total length
+      const int i = h ? 15 - w : w;
       T s = 0;
       for (int k = 0; k <= i; ++k) s = fma(Y[P + 16 + i][P + 16 + k], L[(P >> 1) + k][32 + j], s);
       Y[P + 16 + i][P + j] = -s;
@@ -986,31 +997,28 @@ __global__ void __launch_bounds__(kNT) trsv_inverse_kernel(Args<T> a) {
   }
   __syncthreads();
   // 64x64: W = L[32.., 0..31] inv(A32)   W(i, j) = sum_{k=j..31} L[32+i][k] Y[k][j]
+  // (warp w: columns w, 31-w, 8+w, 23-w; lane i)
   {
-    const int ip = tid >> 4, jq = tid & 15;
+    const int i = lane;
 #pragma unroll
-    for (int hi = 0; hi < 2; ++hi)
-#pragma unroll
-      for (int hj = 0; hj < 2; ++hj) {
-        const int i = hi ? 31 - ip : ip, j = hj ? 31 - jq : jq;
-        T s = 0;
-        for (int k = j; k < 32; ++k) s = fma(L[32 + i][k], Y[k][j], s);
-        L[i][32 + j] = s;
-      }
+    for (int h = 0; h < 4; ++h) {
+      const int j = (h & 1) ? 31 - (w + 8 * (h >> 1)) : w + 8 * (h >> 1);
+      T s = 0;
+      for (int k = j; k < 32; ++k) s = fma(L[32 + i][k], Y[k][j], s);
+      L[i][32 + j] = s;
+    }
   }
   __syncthreads();
-  //   Y[32+i][j] = - sum_{k=0..i} Y[32+i][32+k] W(k, j)
+  //   Y[32+i][j] = - sum_{k=0..i} Y[32+i][32+k] W(k, j)   (warp w: rows w, 31-w, 8+w, 23-w; lane j)
   {
-    const int ip = tid >> 4, jq = tid & 15;
+    const int j = lane;
 #pragma unroll
-    for (int hi = 0; hi < 2; ++hi)
-#pragma unroll
-      for (int hj = 0; hj < 2; ++hj) {
-        const int i = hi ? 31 - ip : ip, j = hj ? 31 - jq : jq;
-        T s = 0;
-        for (int k = 0; k <= i; ++k) s = fma(Y[32 + i][32 + k], L[k][32 + j], s);
-        Y[32 + i][j] = -s;
-      }
+    for (int h = 0; h < 4; ++h) {
+      const int i = (h & 1) ? 31 - (w + 8 * (h >> 1)) : w + 8 * (h >> 1);
+      T s = 0;
+      for (int k = 0; k <= i; ++k) s = fma(Y[32 + i][32 + k], L[k][32 + j], s);
+      Y[32 + i][j] = -s;
+    }
   }
   __syncthreads();
   T *out = const_cast<T *>(a.inv) + K * kTB * kTB;
