@@ -772,8 +772,14 @@ def run_precision(args):
                 ms = timed(fk, 3 if mode == eb.PRECISION_NATIVE else 5)
                 lo = torch.tril(torch.ones(n, n, device="cuda", dtype=torch.bool))
                 rk, mk = A64 @ A64.t(), A64.abs() @ A64.abs().t()
+                # the diagonal sums a_ik^2 (all terms of one sign, no
+                # cancellation) reported apart from the rest of the triangle
+                dg = torch.eye(n, device="cuda", dtype=torch.bool)
+                off = lo & ~dg
                 out[f"ssyrk_{mname}"] = {"ms": round(ms, 3), "tflops": round(flops["ssyrk"] / ms / 1e9, 1),
-                                         **errs(Ck[lo], rk[lo], mk[lo])}
+                                         **errs(Ck[lo], rk[lo], mk[lo]),
+                                         "diagonal": errs(Ck[dg], rk[dg], mk[dg]),
+                                         "off_diagonal": errs(Ck[off], rk[off], mk[off])}
         eb.set_precision(eb.PRECISION_NATIVE)
         del ref_gemm, mag_gemm
     # dgemm: native FP64 DFMA vs Ozaki slice emulation; error on 256 sampled

@@ -35,6 +35,8 @@ template <typename T>
 void nrm2(long n, const T *x, long incx, T *result);
 template <typename T>
 void iamax(long n, const T *x, long incx, size_t *result);
+// dasum with integer significand sums on the bit patterns (level1_ext.cu)
+void dasum_words(long n, const double *x, long incx, double *result);
 }  // namespace l1
 
 namespace l2 {

@@ -252,7 +252,8 @@ void rotm(long n, T *x, long incx, T *y, long incy, const T P[5]) {
 
 // -------------------------------------------------------------- reductions --
 
-// Accumulators.  asum / dot accumulate in the working precision (T); dsdot
+// Accumulators.  sasum / dot accumulate in the working precision (T)
+// (dasum: integer significand sums in level1_ext.cu); dsdot
 // accumulates exact products x*y = p + e (p = fl(x*y), e = fma(x, y, -p))
 // in an unevaluated float pair (hi, lo) updated by TwoSum, so the FP32 pipe
 // carries the per-element work; block and grid sums are native FP64.
@@ -429,7 +430,10 @@ void run_reduce(long n, const typename Acc::In *x, long incx, const typename Acc
 
 template <typename T>
 void asum(long n, const T *x, long incx, T *result) {
-  run_reduce<AsumAcc<T>>(n, x, incx, x, incx, result);
+  if constexpr (sizeof(T) == 8)
+    dasum_words(n, x, incx, result);
+  else
+    run_reduce<AsumAcc<T>>(n, x, incx, x, incx, result);
 }
 template <typename T>
 void dot(long n, const T *x, long incx, const T *y, long incy, T *result) {

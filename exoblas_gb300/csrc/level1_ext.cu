@@ -1,4 +1,5 @@
-// nrm2 and iamax: standard level-1 routines the reference does not have
+// dasum on integer significand sums (below), and nrm2 and iamax:
+// standard level-1 routines the reference does not have
 // (README.md:15 -- Exo lacked the value-dependent control they need), with
 // the reference BLAS semantics (the caller handles N < 1 and, for iamax,
 // incX < 1): iamax returns the 0-based index (as cblas_i?amax) of the first
@@ -466,6 +467,89 @@ __global__ void __launch_bounds__(kT) iamax_kernel(long n, const T *__restrict__
   *result = (x0 != x0 || g.i == LONG_MAX) ? size_t(0) : size_t(g.i);
 }
 
+// dasum (src/level1/asum.py:11-18) with a quarter of the FP64 work: one
+// DADD per element (33.5 M warp lanes at n = 2^25) takes longer on GB300's
+// FP64 unit than reading x from HBM, and the integer path alone keeps the
+// integer ALU 77% busy (ncu; it also occupies the FP64 unit a third of the
+// time), so one element in four takes an FP64 add and the others the
+// integer path.  There |x| is taken apart from its bit pattern
+// (the two 32-bit words that for_each_words hands over, so no FP64 value is
+// held in a register) into its 53-bit significand and biased exponent e, and
+// the significands accumulate in an unsigned 64-bit sum whose least
+// significant bit weighs 2^(E - 1075), E the largest exponent this thread
+// has seen.  A larger exponent shifts the sum down; a sum reaching 2^62 is
+// halved (E + 1) before it could overflow.  Each element or shift truncates
+// less than one unit of the final LSB, which weighs at most 2^-52 max|x|,
+// so the error stays below 2 n eps sum|x|.  Infinities and NaNs go to an
+// FP64 side sum so the IEEE result is kept; the per-thread parts and the
+// block and grid combinations are FP64, in a fixed order.
+struct AsumBits {
+  unsigned long long acc = 0;
+  int E = 1;
+  double special = 0.0;
+  // E stays <= 2046, so an infinity or NaN (e = 2047) always takes the rare
+  // e > E branch; a sum that would need E = 2047 is beyond the FP64 range,
+  // recorded as +inf in the side sum.
+  __device__ __forceinline__ void add(unsigned hi, unsigned lo) {
+    const unsigned h = hi & 0x7fffffffu;
+    int e = int(h >> 20);
+    const unsigned long long m =
+        (static_cast<unsigned long long>((h & 0xfffffu) | (e ? 0x100000u : 0u)) << 32) | lo;
+    e = max(e, 1);  // subnormals: significand without the hidden bit, exponent 1
+    if (e > E) {
+      if (e == 2047) {
+        special += __hiloint2double(int(h), int(lo));
+        return;
+      }
+      acc >>= min(e - E, 63);  // acc < 2^62: a shift by 63 leaves 0
+      E = e;
+    }
+    acc += m >> min(E - e, 63);  // m < 2^53
+    if (acc >> 62) {
+      acc >>= 1;
+      if (E < 2046)
+        ++E;
+      else
+        special = __longlong_as_double(0x7ff0000000000000ll);
+    }
+  }
+  __device__ __forceinline__ double part() const { return ldexp(double(acc), E - 1075) + special; }
+};
+
+__global__ void __launch_bounds__(kT) dasum_kernel(long n, const double *__restrict__ x, long inc, bool vec,
+                                                   double *partials, unsigned *counter, double *result) {
+  __shared__ Part2 sh[kT / 32];
+  __shared__ bool last;
+  // one element in four (the second of the vectors in slots 2 and 3 of the
+  // unrolled loop: known at compile time, so no warp diverges) as one FP64
+  // add, the others on the integer path, so both units share the work
+  AsumBits acc;
+  double sd = 0.0;
+  auto f = [&](int u, unsigned hi, unsigned lo, long i) {
+    if ((u & 2) && (i & 1))
+      sd += fabs(__hiloint2double(int(hi), int(lo)));
+    else
+      acc.add(hi, lo);
+  };
+  words(n, x, inc, vec, f);
+  const Part2 tot = part2_block(acc.part() + sd, 0u, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = tot.ss;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // the last CTA combines the per-CTA partials in CTA order
+  double s = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += kT) s += __ldcg(partials + b);
+  const double g = part2_block(s, 0u, sh).ss;
+  if (threadIdx.x != 0) return;
+  *counter = 0;
+  *result = g;
+}
+
 inline long grid_for(long n, const void *kernel) {
   long blocks = ceil_div(n, long(kT) * 16);
   if (blocks < 1) blocks = 1;
@@ -501,6 +585,18 @@ void iamax(long n, const T *x, long incx, size_t *result) {
   unsigned *counter = zero_words(1);
   iamax_kernel<T><<<int(blocks), kT, 0, ctx().stream>>>(n, x, incx, vec, partials, counter, result);
   EXB_LAUNCH("iamax kernel");
+  count_launch();
+}
+
+void dasum_words(long n, const double *x, long incx, double *result) {
+  using namespace ext;
+  if (n < 0) n = 0;
+  const long blocks = grid_for(n, reinterpret_cast<const void *>(dasum_kernel));
+  const bool vec = incx == 1 && aligned16(x);
+  double *partials = static_cast<double *>(scratch(sizeof(double) * size_t(blocks)));
+  unsigned *counter = zero_words(1);
+  dasum_kernel<<<int(blocks), kT, 0, ctx().stream>>>(n, x, incx, vec, partials, counter, result);
+  EXB_LAUNCH("dasum kernel");
   count_launch();
 }
 
