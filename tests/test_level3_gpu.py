@@ -118,3 +118,92 @@ def test_beta_zero_multiplies_c(cuda, mode):
             assert np.isfinite(C[mask & np.tril(np.ones_like(mask))]).all()
     finally:
         eb.set_precision(0)
+
+
+def _fp32_bound(got, ref, mag, k):
+    """|got - ref| <= 4 (k + 1) eps_s |A||B| componentwise (FP64 reference)."""
+    err = (got.double() - ref).abs()
+    return bool((err <= 4 * (k + 1) * EPS["s"] * mag + 1e-300).all())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ta", [111, 112])
+@pytest.mark.parametrize("tb", [111, 112])
+def test_sgemm_full_tile_path(cuda, ta, tb):
+    """sgemm on the FP32 full-tile path (m, n multiples of 128 with at least
+    one tile per SM, k a multiple of 16), every transpose pair, against FP64."""
+    import exoblas_gb300 as eb
+
+    torch = cuda
+    eb.set_precision(eb.PRECISION_NATIVE)
+    m, n, k = 2048, 1536, 272
+    g = torch.Generator(device="cuda").manual_seed(ta * 7 + tb)
+    A = torch.rand(m * k, device="cuda", generator=g).mul_(2).sub_(1)
+    B = torch.rand(k * n, device="cuda", generator=g).mul_(2).sub_(1)
+    C0 = torch.rand(m * n, device="cuda", generator=g).mul_(2).sub_(1)
+    C = C0.clone()
+    lda, ldb = (k if ta == 111 else m), (n if tb == 111 else k)
+    eb.exo_sgemm(101, ta, tb, m, n, k, 1.25, A, lda, B, ldb, -0.5, C, n)
+    opA = A.view(m, k) if ta == 111 else A.view(k, m).t()
+    opB = B.view(k, n) if tb == 111 else B.view(n, k).t()
+    ref = 1.25 * (opA.double() @ opB.double()) - 0.5 * C0.view(m, n).double()
+    mag = 1.25 * (opA.double().abs() @ opB.double().abs()) + 0.5 * C0.view(m, n).double().abs()
+    assert _fp32_bound(C.view(m, n), ref, mag, k)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("trans", [111, 112])
+def test_ssyrk_full_tile_path(cuda, uplo, trans):
+    """ssyrk on the full-tile path: the triangle against FP64, the other
+    triangle untouched."""
+    import exoblas_gb300 as eb
+
+    torch = cuda
+    eb.set_precision(eb.PRECISION_NATIVE)
+    n, k = 2048, 144
+    g = torch.Generator(device="cuda").manual_seed(uplo + trans)
+    A = torch.rand(n * k, device="cuda", generator=g).mul_(2).sub_(1)
+    C0 = torch.rand(n * n, device="cuda", generator=g).mul_(2).sub_(1)
+    C = C0.clone()
+    eb.exo_ssyrk(101, uplo, trans, n, k, 0.75, A, k if trans == 111 else n, 0.5, C, n)
+    opA = (A.view(n, k) if trans == 111 else A.view(k, n).t()).double()
+    ref = 0.75 * (opA @ opA.t()) + 0.5 * C0.view(n, n).double()
+    mag = 0.75 * (opA.abs() @ opA.abs().t()) + 0.5 * C0.view(n, n).double().abs()
+    tri = torch.triu(torch.ones(n, n, dtype=torch.bool, device="cuda"))
+    if uplo == 122:
+        tri = tri.t()
+    Cv = C.view(n, n)
+    assert _fp32_bound(Cv[tri], ref[tri], mag[tri], k)
+    assert torch.equal(Cv[~tri], C0.view(n, n)[~tri])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("side", [141, 142])
+@pytest.mark.parametrize("uplo", [121, 122])
+def test_ssymm_full_tile_path(cuda, side, uplo):
+    """ssymm on the full-tile path (sym(A) written out from the stored
+    triangle, then the FP32 tiles); the unstored triangle of A holds NaN and
+    must not be read."""
+    import exoblas_gb300 as eb
+
+    torch = cuda
+    eb.set_precision(eb.PRECISION_NATIVE)
+    m, n = 2048, 1280
+    d = m if side == 141 else n
+    g = torch.Generator(device="cuda").manual_seed(side + uplo)
+    A = torch.rand(d, d, device="cuda", generator=g).mul_(2).sub_(1)
+    stored = torch.triu(A) if uplo == 121 else torch.tril(A)
+    S = (stored + stored.t() - torch.diag(torch.diag(A))).double()
+    Anan = A.clone()
+    hidden = torch.tril(torch.ones(d, d, dtype=torch.bool, device="cuda"), -1)
+    Anan[hidden if uplo == 121 else hidden.t()] = float("nan")
+    B = torch.rand(m, n, device="cuda", generator=g).mul_(2).sub_(1)
+    C0 = torch.rand(m, n, device="cuda", generator=g).mul_(2).sub_(1)
+    C = C0.clone()
+    eb.exo_ssymm(101, side, uplo, m, n, 1.5, Anan.flatten(), d, B.flatten(), n, 0.25, C.view(-1), n)
+    Bd = B.double()
+    prod, pmag = (S @ Bd, S.abs() @ Bd.abs()) if side == 141 else (Bd @ S, Bd.abs() @ S.abs())
+    ref = 1.5 * prod + 0.25 * C0.double()
+    mag = 1.5 * pmag + 0.25 * C0.double().abs()
+    assert _fp32_bound(C, ref, mag, d)
