@@ -114,6 +114,8 @@ EXTRA = {
     "exoblas_batch_plan_destroy": ("i", "p"),
     "exoblas_batch_tune": ("i", ""),
     "exoblas_batch_tile_config": ("i", "iii"),
+    "exoblas_batch_set_tensor_cores": ("i", "i"),
+    "exoblas_batch_plan_tensor_core_calls": ("i", "pp"),
     "exoblas_set_column_major": ("i", "i"),
     "exoblas_get_column_major": ("i", ""),
     "exoblas_server_create": ("i", "izzzp"),

@@ -58,6 +58,14 @@ def tile_config(m, n, k) -> int:
     return _native.lib().exoblas_batch_tile_config(m, n, k)
 
 
+def set_tensor_cores(on: bool) -> None:
+    """sgemm calls with m, n, k >= 128 on the tensor cores (split-BF16) in
+    plans created afterwards; off: every call on FFMA work units."""
+    st = _native.lib().exoblas_batch_set_tensor_cores(1 if on else 0)
+    if st:
+        raise ExoBlasError(st, "exoblas_batch_set_tensor_cores")
+
+
 class BatchPlan:
     def __init__(self, ops):
         arr = (BatchOp * len(ops))(*ops)
@@ -72,6 +80,13 @@ class BatchPlan:
         u, f, b = C.c_int(), C.c_double(), C.c_double()
         _native.lib().exoblas_batch_plan_info(self.handle, C.byref(u), C.byref(f), C.byref(b))
         return {"units": u.value, "flops": f.value, "bytes": b.value}
+
+    def tensor_core_calls(self) -> int:
+        n = C.c_int()
+        st = _native.lib().exoblas_batch_plan_tensor_core_calls(self.handle, C.byref(n))
+        if st:
+            raise ExoBlasError(st, "exoblas_batch_plan_tensor_core_calls")
+        return n.value
 
     def run(self):
         st = _native.lib().exoblas_batch_plan_run(self.handle)

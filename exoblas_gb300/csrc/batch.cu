@@ -3,7 +3,11 @@
 // exo_dgemv and exo_strsv semantics, test/level3/gemm/exo_gemm_wrapper.h,
 // test/level2/gemv/exo_gemv_wrapper.h, test/level2/trsv/exo_trsv_wrapper.h).
 //
-// A plan turns the calls into work units, each small enough for one CTA:
+// sgemm calls of at least 128 in m, n and k run on the tensor cores instead:
+// one grouped split-BF16 product over all of them (gemm_tc.cu), launched
+// before the persistent kernel; each gives the bits of exo_sgemm on the
+// split-BF16 path.  A plan turns the other calls into work units, each
+// small enough for one CTA:
 //   GEMM_TILE   one TM x TN tile of one sgemm, TM x TN chosen per call by the
 //               autotuner (32x32, 64x64 or 128x128)
 //   GEMV_ROWS   128 rows of a NoTrans dgemv / 64 columns of a Trans dgemv
@@ -29,6 +33,7 @@
 
 #include "batch.h"
 #include "common.cuh"
+#include "kernels.h"
 #include "runtime.h"
 
 namespace exb {
@@ -487,8 +492,19 @@ static int launch_units(const Op *dops, const Unit *dunits, int nunits, int *tic
 }
 
 // ------------------------------------------------------------------ plan ---
+// sgemm calls of at least kTcMN in m and n and kTcK in k go to the tensor
+// cores as one grouped split-BF16 product (l3::tc_group_*) unless switched
+// off; the rest become work units of the persistent kernel.
+static bool g_tensor_cores = true;
+constexpr int kTcMN = 128, kTcK = 128;
+static bool tc_eligible(const exoblas_batch_op &b) {
+  return g_tensor_cores && b.op == EXOBLAS_BATCH_SGEMM && b.m >= kTcMN && b.n >= kTcMN && b.k >= kTcK;
+}
+
 struct Plan {
   int device = 0;
+  l3::TcGroup *tc = nullptr;  // sgemm calls on the tensor cores
+  int ntc = 0;
   Op *ops = nullptr;
   Unit *units = nullptr;
   int *ticket = nullptr;
@@ -664,6 +680,7 @@ int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_ba
     Context &c = ctx();
     std::vector<bt::Op> dops(count);
     std::vector<std::pair<double, bt::Unit>> us;
+    std::vector<l3::TcGroupOp> tcops;
     double flops = 0, bytes = 0;
     for (int i = 0; i < count; ++i) {
       const exoblas_batch_op &b = ops[i];
@@ -700,6 +717,15 @@ int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_ba
         default:
           fail(EXOBLAS_INVALID_VALUE, "unknown batch op");
       }
+      if (bt::tc_eligible(b)) {
+        tcops.push_back(l3::TcGroupOp{b.flags[0] != 111, b.flags[1] != 111, b.m, b.n, b.k, float(b.alpha),
+                                      float(b.beta), static_cast<const float *>(b.A), long(b.lda),
+                                      static_cast<const float *>(b.B), long(b.ldb), static_cast<float *>(b.C),
+                                      long(b.ldc)});
+        flops += 2.0 * b.m * b.n * b.k;
+        bytes += 4.0 * (double(b.m) * b.k + double(b.k) * b.n + 2.0 * b.m * b.n);
+        continue;
+      }
       bt::add_units(o, i, us, flops, bytes);
     }
     // longest first; ties keep submission order (stable)
@@ -731,6 +757,18 @@ int exoblas_batch_plan_create(const exoblas_batch_op *ops, int count, exoblas_ba
       EXB_CUDA(cudaMemcpyAsync(p->units, units.data(), sizeof(bt::Unit) * units.size(), cudaMemcpyHostToDevice,
                                c.stream));
     EXB_CUDA(cudaStreamSynchronize(c.stream));
+    if (!tcops.empty()) {
+      try {
+        p->tc = l3::tc_group_create(tcops.data(), int(tcops.size()));
+      } catch (...) {
+        cudaFree(p->ops);
+        cudaFree(p->units);
+        cudaFree(p->ticket);
+        delete p;
+        throw;
+      }
+      p->ntc = int(tcops.size());
+    }
     *out = reinterpret_cast<exoblas_batch_plan>(p);
   });
 }
@@ -741,6 +779,7 @@ int exoblas_batch_plan_run(exoblas_batch_plan plan) {
     if (!p) fail(EXOBLAS_INVALID_VALUE, "NULL plan");
     Context &c = ctx();
     if (c.device != p->device) fail(EXOBLAS_INVALID_VALUE, "plan belongs to another device");
+    if (p->tc) l3::tc_group_launch(p->tc, c.stream);
     bt::launch_units(p->ops, p->units, p->nunits, p->ticket, c.stream, c.sm_count);
     if (c.blocking) EXB_CUDA(cudaStreamSynchronize(c.stream));
   });
@@ -752,9 +791,13 @@ int exoblas_batch_plan_graph_launch(exoblas_batch_plan plan) {
     if (!p) fail(EXOBLAS_INVALID_VALUE, "NULL plan");
     Context &c = ctx();
     if (!p->exec) {
-      // capture one run (ticket reset + persistent kernel) on a private stream
+      // capture one run (tensor-core group, ticket reset + persistent
+      // kernel) on a private stream; the status word the group's kernel
+      // reports to is allocated first (no allocation while capturing)
+      (void)device_status_word();
       EXB_CUDA(cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking));
       EXB_CUDA(cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal));
+      if (p->tc) l3::tc_group_launch(p->tc, p->graph_stream);
       bt::launch_units(p->ops, p->units, p->nunits, p->ticket, p->graph_stream, c.sm_count);
       EXB_CUDA(cudaStreamEndCapture(p->graph_stream, &p->graph));
       EXB_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
@@ -782,10 +825,23 @@ int exoblas_batch_plan_destroy(exoblas_batch_plan plan) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->graph_stream) cudaStreamDestroy(p->graph_stream);
+    l3::tc_group_destroy(p->tc);
     cudaFree(p->ops);
     cudaFree(p->units);
     cudaFree(p->ticket);
     delete p;
+  });
+}
+
+int exoblas_batch_set_tensor_cores(int on) {
+  return guarded("exoblas_batch_set_tensor_cores", [&] { bt::g_tensor_cores = on != 0; });
+}
+
+int exoblas_batch_plan_tensor_core_calls(exoblas_batch_plan plan, int *calls) {
+  return guarded("exoblas_batch_plan_tensor_core_calls", [&] {
+    bt::Plan *p = reinterpret_cast<bt::Plan *>(plan);
+    if (!p || !calls) fail(EXOBLAS_INVALID_VALUE, "NULL argument");
+    *calls = p->ntc;
   });
 }
 

@@ -23,7 +23,8 @@
 //                (M = 128, N = 128, K = 16) and tcgen05.commit
 //   warps 2..17  epilogue: per chunk, tcgen05.ld of both accumulators of a
 //                buffer (four warps per 32-lane quarter, 32 columns each);
-//                per tile, beta * C fused into the store (syrk: elements
+//                per tile, beta * C fused into the store, C accessed in
+//                32-byte row segments through shared memory (syrk: elements
 //                outside the triangle are left alone)
 // Synchronisation is by mbarriers; every wait is bounded by a clock budget
 // after which the CTA records a timeout in the device status word, drains
@@ -32,7 +33,9 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -52,6 +55,8 @@ constexpr int kEpiWarps = 16;
 constexpr int kEpiCols = BN / (kEpiWarps / 4);  // columns per epilogue warp
 constexpr int kThreads = 64 + 32 * kEpiWarps;
 constexpr int kChunkKB = 4;      // k-blocks per accumulation chunk (K = 256)
+constexpr int kEpiSmem = kEpiWarps * 32 * 9 * 4;  // per epilogue warp: 32 rows x 8 columns, row pitch 9
+constexpr int kDynSmem = kStages * kStageBytes + 1024 + kEpiSmem;
 constexpr int kTmemCols = 512;   // two buffers x (hi at column 0, lo at BN)
 
 // products in issue order (small to large); acc 1 = lo, 0 = hi
@@ -95,10 +100,88 @@ __device__ __forceinline__ void tile_coords(const Params &p, int t, int &mt, int
   nt = in / gm;
 }
 
-// ---------------------------------------------------------------- kernel --
-__global__ void __launch_bounds__(kThreads, 1)
-    split_bf16_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-                           Params p) {
+// A group of independent products for split_bf16_group_kernel: per
+// product its two tensor maps (slice planes) and epilogue parameters; per
+// output tile an item (product, m-tile, n-tile).
+struct alignas(128) TcGroupGemm {
+  CUtensorMap ma, mb;
+  int M, N, Mp, Np, kblocks;
+  float alpha, beta;
+  float *C;
+  long ldc;
+};
+struct TcItem {
+  int g, mt, nt, pad;
+};
+
+// What each role needs to know about output tile t of its sequence: the
+// operands' tensor maps and slice pitches, the tile's origin, its k-blocks
+// and the epilogue's parameters.
+struct TileRef {
+  const CUtensorMap *ma, *mb;
+  int Mp, Np;      // slice row pitches of the two planes
+  int am, bn;      // tile origin: rows am.. of op(A), columns bn.. of op(B)
+  int kblocks;
+  int M, N, tri;
+  float alpha, beta;
+  float *C;
+  long ldc;
+};
+
+// One product (split_bf16_gemm_kernel): tiles in grouped raster order.
+struct SingleSrc {
+  const CUtensorMap *ma, *mb;
+  const Params *p;
+  __device__ __forceinline__ void tile(int t, TileRef &r) const {
+    int mt, nt;
+    tile_coords(*p, t, mt, nt);
+    r.ma = ma;
+    r.mb = mb;
+    r.Mp = p->Mp;
+    r.Np = p->Np;
+    r.am = mt * BM;
+    r.bn = nt * BN;
+    r.kblocks = p->kblocks;
+    r.M = p->M;
+    r.N = p->N;
+    r.tri = p->tri;
+    r.alpha = p->alpha;
+    r.beta = p->beta;
+    r.C = p->C;
+    r.ldc = p->ldc;
+  }
+};
+
+// A group of independent products (split_bf16_group_kernel): each item is
+// one output tile of one product, items longest first.
+struct GroupSrc {
+  const TcGroupGemm *gg;
+  const TcItem *items;
+  __device__ __forceinline__ void tile(int t, TileRef &r) const {
+    const TcItem it = items[t];
+    const TcGroupGemm &g = gg[it.g];
+    r.ma = &g.ma;
+    r.mb = &g.mb;
+    r.Mp = g.Mp;
+    r.Np = g.Np;
+    r.am = it.mt * BM;
+    r.bn = it.nt * BN;
+    r.kblocks = g.kblocks;
+    r.M = g.M;
+    r.N = g.N;
+    r.tri = 0;
+    r.alpha = g.alpha;
+    r.beta = g.beta;
+    r.C = g.C;
+    r.ldc = g.ldc;
+  }
+};
+
+// ------------------------------------------------------------------ body --
+// The persistent tile loop shared by both kernels: tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... of the source's ntiles.
+template <class Src>
+__device__ __forceinline__ void tc_body(const Src &src, int ntiles, int *status) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned stage area (128B-swizzle atoms need it)
   unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -130,22 +213,26 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (warp == 0) {
     // ------------------------------------------------------ TMA producer --
     if (lane == 0) {
-      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
-      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
       int stage = 0;
       uint32_t round = 0;
       long issued = 0;
-      for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
-        int mt, nt;
-        tile_coords(p, t, mt, nt);
-        for (int kb = 0; kb < p.kblocks; ++kb) {
-          if (!mbar_wait(&empty[stage], (round & 1) ^ 1, &abort_flag, p.status)) break;
+      const CUtensorMap *last_ma = nullptr;
+      for (int t = blockIdx.x; t < ntiles && !abort_flag; t += gridDim.x) {
+        TileRef r;
+        src.tile(t, r);
+        if (r.ma != last_ma) {
+          asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(r.ma)) : "memory");
+          asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(r.mb)) : "memory");
+          last_ma = r.ma;
+        }
+        for (int kb = 0; kb < r.kblocks; ++kb) {
+          if (!mbar_wait(&empty[stage], (round & 1) ^ 1, &abort_flag, status)) break;
           mbar_expect_tx(&full[stage], kStageBytes);
           unsigned char *st = smem + stage * kStageBytes;
 #pragma unroll
           for (int s = 0; s < kSlices; ++s) {
-            tma_load_2d(st + s * kTileBytes, &mapA, &full[stage], kb * BK, s * p.Mp + mt * BM);
-            tma_load_2d(st + (kSlices + s) * kTileBytes, &mapB, &full[stage], kb * BK, s * p.Np + nt * BN);
+            tma_load_2d(st + s * kTileBytes, r.ma, &full[stage], kb * BK, s * r.Mp + r.am);
+            tma_load_2d(st + (kSlices + s) * kTileBytes, r.mb, &full[stage], kb * BK, s * r.Np + r.bn);
           }
           ++issued;
           if (++stage == kStages) {
@@ -172,15 +259,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       uint32_t round = 0;
       uint32_t chunk = 0;  // global chunk counter: buffer chunk & 1
       bool any = false;
-      for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
-        for (int kb0 = 0; kb0 < p.kblocks && !abort_flag; kb0 += kChunkKB) {
+      for (int t = blockIdx.x; t < ntiles && !abort_flag; t += gridDim.x) {
+        TileRef r;
+        src.tile(t, r);
+        for (int kb0 = 0; kb0 < r.kblocks && !abort_flag; kb0 += kChunkKB) {
           const int buf = int(chunk & 1);
-          if (!mbar_wait(&accempty[buf], ((chunk >> 1) & 1) ^ 1, &abort_flag, p.status)) break;
+          if (!mbar_wait(&accempty[buf], ((chunk >> 1) & 1) ^ 1, &abort_flag, status)) break;
           tc_fence_after();
           const uint32_t accbase = tmem + uint32_t(buf * 2 * BN);
-          const int kb1 = kb0 + kChunkKB < p.kblocks ? kb0 + kChunkKB : p.kblocks;
+          const int kb1 = kb0 + kChunkKB < r.kblocks ? kb0 + kChunkKB : r.kblocks;
           for (int kb = kb0; kb < kb1; ++kb) {
-            if (!mbar_wait(&full[stage], round & 1, &abort_flag, p.status)) break;
+            if (!mbar_wait(&full[stage], round & 1, &abort_flag, status)) break;
             tc_fence_after();
             const uint32_t sbase = smem_u32(smem + stage * kStageBytes);
 #pragma unroll
@@ -220,16 +309,16 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int part = (warp - 2) >> 2;       // columns [kEpiCols part, kEpiCols (part + 1))
     const int row = q * 32 + lane;
     uint32_t chunk = 0;
-    for (int t = blockIdx.x; t < p.tiles && !abort_flag; t += gridDim.x) {
-      int mt, nt;
-      tile_coords(p, t, mt, nt);
+    for (int t = blockIdx.x; t < ntiles && !abort_flag; t += gridDim.x) {
+      TileRef r;
+      src.tile(t, r);
       float sum[kEpiCols], comp[kEpiCols];
 #pragma unroll
       for (int j = 0; j < kEpiCols; ++j) sum[j] = comp[j] = 0.f;
       bool ok = true;
-      for (int kb0 = 0; kb0 < p.kblocks; kb0 += kChunkKB) {
+      for (int kb0 = 0; kb0 < r.kblocks; kb0 += kChunkKB) {
         const int buf = int(chunk & 1);
-        if (!mbar_wait(&accfull[buf], (chunk >> 1) & 1, &abort_flag, p.status)) {
+        if (!mbar_wait(&accfull[buf], (chunk >> 1) & 1, &abort_flag, status)) {
           ok = false;
           break;
         }
@@ -256,16 +345,28 @@ __global__ void __launch_bounds__(kThreads, 1)
         ++chunk;
       }
       if (!ok) break;
-      const long gi = long(mt) * BM + row;
-      if (gi < p.M) {
-        float *crow = p.C + gi * p.ldc;
-        const long gj0 = long(nt) * BN + part * kEpiCols;
+      // C is read and written through shared memory in 32-byte row segments:
+      // per 8 columns, lane `row` stores alpha * sum of its 8 elements, then
+      // lane l takes row 4i + l/8, column l%8 (i = 0..7).  (A lane per row
+      // touched 32 lines per warp access: 31 sectors per request.)
+      float *cs = reinterpret_cast<float *>(smem + kStages * kStageBytes) + (warp - 2) * (32 * 9);
+      const long grow0 = long(r.am) + q * 32, gcol0 = long(r.bn) + part * kEpiCols;
 #pragma unroll
-        for (int j = 0; j < kEpiCols; ++j) {
-          const long gj = gj0 + j;
-          const bool in = gj < p.N && !(p.tri == 1 && gj > gi) && !(p.tri == 2 && gj < gi);
-          if (in) crow[gj] = p.alpha * (sum[j] + comp[j]) + p.beta * crow[gj];
+      for (int c8 = 0; c8 < kEpiCols; c8 += 8) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) cs[lane * 9 + j] = r.alpha * (sum[c8 + j] + comp[c8 + j]);
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int rr = 4 * i + (lane >> 3), cc = lane & 7;
+          const long gi = grow0 + rr, gj = gcol0 + c8 + cc;
+          const bool in = gi < r.M && gj < r.N && !(r.tri == 1 && gj > gi) && !(r.tri == 2 && gj < gi);
+          if (in) {
+            float *cp = r.C + gi * r.ldc + gj;
+            *cp = cs[rr * 9 + cc] + r.beta * *cp;
+          }
         }
+        __syncwarp();
       }
     }
   }
@@ -277,14 +378,29 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------- kernels --
+__global__ void __launch_bounds__(kThreads, 1)
+    split_bf16_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                           Params p) {
+  const SingleSrc src{&mapA, &mapB, &p};
+  tc_body(src, p.tiles, p.status);
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    split_bf16_group_kernel(const TcGroupGemm *__restrict__ gg, const TcItem *__restrict__ items, int nitems,
+                            int *status) {
+  const GroupSrc src{gg, items};
+  tc_body(src, nitems, status);
+}
+
 // --------------------------------------------------------------- split ----
 // out[s][r][k] (s < 3, r < Rp, k < Kp, bf16) for the logical rows x K operand
 // X(r, k); zero outside rows x K.  32 x 32 tiles through shared memory so
 // both the source (either orientation) and the K-major output are coalesced.
 template <class Op>
-__global__ void split3_kernel(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out) {
+__device__ __forceinline__ void split3_tile(const Op &X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out, int r0,
+                                            int k0) {
   __shared__ float tile[32][33];
-  const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
   const bool src_k_fast = X.k_contiguous();
   for (int i = ty; i < 32; i += 8) {
@@ -315,6 +431,11 @@ __global__ void split3_kernel(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat
   }
 }
 
+template <class Op>
+__global__ void split3_kernel(Op X, int rows, int K, int Rp, int Kp, __nv_bfloat16 *out) {
+  split3_tile(X, rows, K, Rp, Kp, out, int(blockIdx.y) * 32, int(blockIdx.x) * 32);
+}
+
 // operand views: X(r, k) for the logical rows x K operand
 struct ViewPlain {
   const float *p;
@@ -339,6 +460,29 @@ struct ViewSym {
   }
   __device__ bool k_contiguous() const { return true; }
 };
+
+// Grouped split: job j slices one operand of one product (ViewPlain) into
+// its three planes; the grid's blocks are the jobs' 32 x 32 tiles in job
+// order, first[j] the first block of job j.
+struct SplitJob {
+  ViewPlain x;
+  int rows, K, Rp, Kp;
+  __nv_bfloat16 *out;
+  long first;
+};
+__global__ void split3_group_kernel(const SplitJob *__restrict__ jobs, int njobs) {
+  const long b = blockIdx.x;
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].first <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const SplitJob &J = jobs[lo];
+  const long local = b - J.first;
+  const int kt = (J.Kp + 31) / 32;
+  split3_tile(J.x, J.rows, J.K, J.Rp, J.Kp, J.out, int(local / kt) * 32, int(local % kt) * 32);
+}
 
 // ---------------------------------------------------------------- host ----
 template <class Op>
@@ -383,7 +527,7 @@ static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, floa
   p.ldc = ldc;
   p.status = device_status_word();
   static std::once_flag attr[64];
-  const int smem = kStages * kStageBytes + 1024;
+  const int smem = kDynSmem;
   const int dev = c.device < 64 ? c.device : 63;
   std::call_once(attr[dev], [smem] {
     EXB_CUDA(cudaFuncSetAttribute(split_bf16_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -393,6 +537,130 @@ static void run(OA xa, OB xb, int M, int N, int K, float alpha, float beta, floa
   EXB_LAUNCH("split-bf16 tcgen05 gemm kernel");
   count_launch();
   c.status_pending = true;
+}
+
+// A group of sgemm products on the tensor cores: slice planes, split jobs,
+// per-product tensor maps and the tile items, built once and kept on the
+// device; a launch runs the grouped split and the grouped product.
+constexpr int kGroupSmem = kDynSmem;
+
+struct TcGroupState {
+  TcGroupGemm *gg = nullptr;
+  TcItem *items = nullptr;
+  SplitJob *jobs = nullptr;
+  __nv_bfloat16 *planes = nullptr;
+  int nitems = 0, njobs = 0;
+  long split_blocks = 0;
+};
+
+static TcGroupState *group_create(const TcGroupOp *ops, int n) {
+  // launch set-up done here, outside any stream capture of the launches
+  {
+    static std::once_flag attr[64];
+    const int dev = ctx().device < 64 ? ctx().device : 63;
+    std::call_once(attr[dev], [] {
+      EXB_CUDA(cudaFuncSetAttribute(split_bf16_group_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kGroupSmem));
+    });
+    (void)device_status_word();
+  }
+  std::vector<TcGroupGemm> gg(n);
+  std::vector<SplitJob> jobs;
+  std::vector<std::pair<int, TcItem>> items;  // (k-blocks, item)
+  std::vector<size_t> aoff(n), boff(n);
+  size_t total = 0;
+  for (int g = 0; g < n; ++g) {
+    const TcGroupOp &o = ops[g];
+    const int Kp = round_up(o.k, BK), Mp = round_up(o.m, BM), Np = round_up(o.n, BN);
+    aoff[g] = total;
+    total += size_t(kSlices) * Mp * Kp;
+    boff[g] = total;
+    total += size_t(kSlices) * Np * Kp;
+  }
+  TcGroupState *st = new TcGroupState();
+  cudaError_t e = cudaMalloc(&st->planes, (total ? total : 1) * 2);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete st;
+    fail(EXOBLAS_ALLOC_FAILED, "tensor-core batch: slice planes");
+  }
+  long first = 0;
+  for (int g = 0; g < n; ++g) {
+    const TcGroupOp &o = ops[g];
+    const int Kp = round_up(o.k, BK), Mp = round_up(o.m, BM), Np = round_up(o.n, BN);
+    __nv_bfloat16 *pa = st->planes + aoff[g], *pb = st->planes + boff[g];
+    // op(B) is k x n; its K-major form is row j, column kk = op(B)[kk][j]
+    const SplitJob ja{ViewPlain{o.A, o.lda, o.ta}, o.m, o.k, Mp, Kp, pa, first};
+    first += long(Mp / 32) * ((Kp + 31) / 32);
+    const SplitJob jb{ViewPlain{o.B, o.ldb, !o.tb}, o.n, o.k, Np, Kp, pb, first};
+    first += long(Np / 32) * ((Kp + 31) / 32);
+    jobs.push_back(ja);
+    jobs.push_back(jb);
+    TcGroupGemm &q = gg[g];
+    q.ma = make_map(pa, long(kSlices) * Mp, Kp, BK, BM);
+    q.mb = make_map(pb, long(kSlices) * Np, Kp, BK, BN);
+    q.M = o.m;
+    q.N = o.n;
+    q.Mp = Mp;
+    q.Np = Np;
+    q.kblocks = Kp / BK;
+    q.alpha = o.alpha;
+    q.beta = o.beta;
+    q.C = o.C;
+    q.ldc = o.ldc;
+    for (int mt = 0; mt < Mp / BM; ++mt)
+      for (int nt = 0; nt < Np / BN; ++nt) items.push_back({q.kblocks, TcItem{g, mt, nt, 0}});
+  }
+  // longest tiles first; ties keep product and raster order (stable)
+  std::stable_sort(items.begin(), items.end(),
+                   [](const std::pair<int, TcItem> &a, const std::pair<int, TcItem> &b) { return a.first > b.first; });
+  std::vector<TcItem> it(items.size());
+  for (size_t i = 0; i < items.size(); ++i) it[i] = items[i].second;
+  st->nitems = int(it.size());
+  st->njobs = int(jobs.size());
+  st->split_blocks = first;
+  e = cudaMalloc(&st->gg, sizeof(TcGroupGemm) * (n ? n : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&st->items, sizeof(TcItem) * (it.empty() ? 1 : it.size()));
+  if (e == cudaSuccess) e = cudaMalloc(&st->jobs, sizeof(SplitJob) * (jobs.empty() ? 1 : jobs.size()));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(st->planes);
+    cudaFree(st->gg);
+    cudaFree(st->items);
+    cudaFree(st->jobs);
+    delete st;
+    fail(EXOBLAS_ALLOC_FAILED, "tensor-core batch: tables");
+  }
+  Context &c = ctx();
+  if (n) EXB_CUDA(cudaMemcpyAsync(st->gg, gg.data(), sizeof(TcGroupGemm) * n, cudaMemcpyHostToDevice, c.stream));
+  if (!it.empty())
+    EXB_CUDA(cudaMemcpyAsync(st->items, it.data(), sizeof(TcItem) * it.size(), cudaMemcpyHostToDevice, c.stream));
+  if (!jobs.empty())
+    EXB_CUDA(cudaMemcpyAsync(st->jobs, jobs.data(), sizeof(SplitJob) * jobs.size(), cudaMemcpyHostToDevice, c.stream));
+  EXB_CUDA(cudaStreamSynchronize(c.stream));
+  return st;
+}
+
+static int group_launch(const TcGroupState *st, cudaStream_t s) {
+  if (!st || st->nitems == 0) return 0;
+  Context &c = ctx();
+  split3_group_kernel<<<unsigned(st->split_blocks), 256, 0, s>>>(st->jobs, st->njobs);
+  EXB_LAUNCH("grouped bf16 split kernel");
+  const int smem = kGroupSmem;
+  const int grid = st->nitems < c.sm_count ? st->nitems : c.sm_count;
+  split_bf16_group_kernel<<<grid, kThreads, smem, s>>>(st->gg, st->items, st->nitems, device_status_word());
+  EXB_LAUNCH("grouped split-bf16 tcgen05 gemm kernel");
+  c.status_pending = true;
+  return 2;
+}
+
+static void group_destroy(TcGroupState *st) {
+  if (!st) return;
+  cudaFree(st->planes);
+  cudaFree(st->gg);
+  cudaFree(st->items);
+  cudaFree(st->jobs);
+  delete st;
 }
 
 }  // namespace t5
@@ -432,6 +700,16 @@ void syr2k_split_bf16(bool upper, bool trans, long n, long k, float alpha, const
   t5::run(t5::ViewCat{a, b, int(k)}, t5::ViewCat{b, a, int(k)}, int(n), int(n), int(2 * k), alpha, beta, C, ldc,
           upper ? 2 : 1, false);
 }
+
+TcGroup *tc_group_create(const TcGroupOp *ops, int n) {
+  return reinterpret_cast<TcGroup *>(t5::group_create(ops, n));
+}
+int tc_group_launch(const TcGroup *g, cudaStream_t s) {
+  const int k = t5::group_launch(reinterpret_cast<const t5::TcGroupState *>(g), s);
+  count_launch(k);
+  return k;
+}
+void tc_group_destroy(TcGroup *g) { t5::group_destroy(reinterpret_cast<t5::TcGroupState *>(g)); }
 
 }  // namespace l3
 }  // namespace exb

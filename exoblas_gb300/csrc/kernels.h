@@ -103,6 +103,27 @@ bool dsyrk_ozaki(bool upper, bool trans, long n, long k, double alpha, const dou
                  double *C, long ldc);
 bool dsyr2k_ozaki(bool upper, bool trans, long n, long k, double alpha, const double *A, long lda, const double *B,
                   long ldb, double beta, double *C, long ldc);
+// A group of independent FP32 products C_g = alpha_g op(A_g) op(B_g) +
+// beta_g C_g on the split-BF16 tensor-core path (gemm_tc.cu): built once
+// (slice planes, tensor maps, tile items on the device), launched as one
+// grouped split and one grouped persistent product on a stream.  Each
+// product's result equals gemm_split_bf16 of the same call bit for bit.
+struct TcGroupOp {
+  bool ta, tb;
+  int m, n, k;
+  float alpha, beta;
+  const float *A;
+  long lda;
+  const float *B;
+  long ldb;
+  float *C;
+  long ldc;
+};
+struct TcGroup;
+TcGroup *tc_group_create(const TcGroupOp *ops, int n);
+int tc_group_launch(const TcGroup *g, cudaStream_t s);  // returns the kernels launched
+void tc_group_destroy(TcGroup *g);
+
 }  // namespace l3
 
 }  // namespace exb

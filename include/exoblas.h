@@ -311,8 +311,9 @@ EXOBLAS_API void exo_strmm(const enum CBLAS_ORDER Order, const enum CBLAS_SIDE S
  *   STRSV: flags = {Uplo, TransA, Diag}, m = N (<= 4096), A/lda, C = X (ldc = incX) (float)
  * Semantics per call are those of the corresponding exo_* entry point.  A
  * plan uploads the calls once; runs queue one persistent kernel on the
- * thread's stream (blocking mode waits for it); graph launches replay a
- * captured CUDA graph of that run.  sgemm tile shapes come from the
+ * thread's stream (blocking mode waits for it), after the grouped
+ * tensor-core product of the large sgemm calls (below); graph launches
+ * replay a captured CUDA graph of that run.  sgemm tile shapes come from the
  * autotuner (exoblas_batch_tune; cached in the JSON file named by
  * EXOBLAS_TUNE_CACHE when set). */
 enum EXOBLAS_BATCH_OPCODE { EXOBLAS_BATCH_SGEMM = 1, EXOBLAS_BATCH_DGEMV = 2, EXOBLAS_BATCH_STRSV = 3 };
@@ -337,6 +338,14 @@ EXOBLAS_API int exoblas_batch_plan_destroy(exoblas_batch_plan plan);
 EXOBLAS_API int exoblas_batch_tune(void);
 /* tile configuration the autotuner picked for an sgemm of this shape (0: 32x32, 1: 64x64, 2: 128x128) */
 EXOBLAS_API int exoblas_batch_tile_config(int m, int n, int k);
+/* sgemm calls with m, n and k all >= 128 run on the tensor cores, as one
+ * grouped split-BF16 product per plan (FP32 operands as three BF16 terms
+ * each, the exo_sgemm split-BF16 path: error at or below FFMA's); on by
+ * default.  Off: every call on the FFMA work units.  Applies to plans created
+ * afterwards (process-wide). */
+EXOBLAS_API int exoblas_batch_set_tensor_cores(int on);
+/* number of the plan's calls on the tensor cores */
+EXOBLAS_API int exoblas_batch_plan_tensor_core_calls(exoblas_batch_plan plan, int *calls);
 
 /* ------------------------------------------------------------- serving --- */
 /* A request server with continuous batching (no counterpart in the

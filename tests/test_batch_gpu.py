@@ -178,3 +178,97 @@ def test_full_batch_every_instance(cuda):
     for i, (o, r) in enumerate(zip(outs, ran)):
         assert torch.equal(o, r), f"instance {i}: graph replay differs from the plan run"
     plan.close()
+
+
+def _tc_cases(seed=21):
+    """sgemm calls of which most reach the tensor-core group (m, n, k >= 128),
+    all four transpose pairs, ragged sizes (not multiples of 128 or 64)."""
+    g = np.random.default_rng(seed)
+    cases = []
+    for i, (m, n, k) in enumerate([(128, 128, 128), (300, 200, 130), (129, 640, 257), (1000, 130, 700),
+                                   (96, 512, 512), (256, 256, 31), (517, 389, 1021), (63, 1999, 128),
+                                   (64, 64, 32), (70, 1030, 40)]):
+        ta, tb = (NT, TR)[i % 2], (NT, TR)[(i // 2) % 2]
+        ar, ac = (m, k) if ta == NT else (k, m)
+        br, bc = (k, n) if tb == NT else (n, k)
+        A = g.uniform(-1, 1, ar * ac).astype(np.float32)
+        B = g.uniform(-1, 1, br * bc).astype(np.float32)
+        Cm = g.uniform(-1, 1, m * n).astype(np.float32)
+        cases.append(Case("sgemm", [ROW, ta, tb, m, n, k, 1.25, A, ac, B, bc, -0.5, Cm, n], [12], nred=k + 1))
+    return cases
+
+
+@pytest.mark.gpu
+def test_tensor_core_group_matches_split_bf16_sgemm(cuda):
+    """Calls of at least 128 in m, n and k run in the grouped tensor-core
+    product and give exo_sgemm's split-BF16 bits; the others stay on the
+    FFMA units; every call within the FP32 bound; with the tensor cores
+    switched off no call goes there."""
+    import exoblas_gb300 as eb
+    from exoblas_gb300 import batch
+
+    torch = cuda
+    cases = _tc_cases()
+    eligible = [c.args[3] >= 128 and c.args[4] >= 128 and c.args[5] >= 128 for c in cases]
+    ops, dev = _to_ops(torch, cases)
+    plan = batch.BatchPlan(ops)
+    assert plan.tensor_core_calls() == sum(eligible)
+    plan.run()
+    torch.cuda.synchronize()
+    outs = [d[12].cpu().numpy() for d in dev]
+    plan.close()
+    for c, got, tc in zip(cases, outs, eligible):
+        _check(c, got)
+        if tc:
+            # the same call alone on the split-BF16 path
+            a = [torch.from_numpy(v.copy()).cuda() if isinstance(v, np.ndarray) else v for v in c.args]
+            eb.set_precision(eb.PRECISION_SPLIT_BF16)
+            try:
+                eb.exo_sgemm(*a)
+            finally:
+                eb.set_precision(eb.PRECISION_NATIVE)
+            assert a[12].cpu().numpy().tobytes() == got.tobytes(), f"{c.args[3:6]}: group differs from exo_sgemm"
+    batch.set_tensor_cores(False)
+    try:
+        ops2, _ = _to_ops(torch, cases)
+        plan2 = batch.BatchPlan(ops2)
+        assert plan2.tensor_core_calls() == 0
+        plan2.close()
+    finally:
+        batch.set_tensor_cores(True)
+
+
+@pytest.mark.gpu
+def test_graph_launch_first_on_a_fresh_thread(cuda):
+    """A plan whose first use is a graph launch, on a thread that has not
+    called the library before (nothing allocated yet in its context): the
+    capture must not allocate, and the replay equals a plain run."""
+    import threading
+
+    from exoblas_gb300 import batch
+
+    torch = cuda
+    cases = _tc_cases(seed=5)[:4]
+    ops, dev = _to_ops(torch, cases)
+    box = {}
+
+    def body():
+        try:
+            torch.cuda.set_device(0)
+            plan = batch.BatchPlan(ops)
+            plan.graph_launch()
+            torch.cuda.synchronize()
+            box["graph"] = [d[12].clone() for d in dev]
+            plan.run()
+            torch.cuda.synchronize()
+            box["run"] = [d[12].clone() for d in dev]
+            plan.close()
+        except Exception as e:  # reported on the main thread
+            box["error"] = e
+
+    t = threading.Thread(target=body)
+    t.start()
+    t.join()
+    assert "error" not in box, box.get("error")
+    for c, g in zip(cases, box["graph"]):
+        _check(c, g.cpu().numpy())
