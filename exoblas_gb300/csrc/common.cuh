@@ -49,6 +49,7 @@ struct Arena {
 struct Context {
   int device = 0;
   int sm_count = 0;
+  bool pageable_direct = false;  // the device reads pageable host memory through the host page tables
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   bool blocking = true;
