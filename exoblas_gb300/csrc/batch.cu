@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -495,7 +496,7 @@ static int launch_units(const Op *dops, const Unit *dunits, int nunits, int *tic
 // sgemm calls of at least kTcMN in m and n and kTcK in k go to the tensor
 // cores as one grouped split-BF16 product (l3::tc_group_*) unless switched
 // off; the rest become work units of the persistent kernel.
-static bool g_tensor_cores = true;
+static std::atomic<bool> g_tensor_cores{true};
 constexpr int kTcMN = 128, kTcK = 128;
 static bool tc_eligible(const exoblas_batch_op &b) {
   return g_tensor_cores && b.op == EXOBLAS_BATCH_SGEMM && b.m >= kTcMN && b.n >= kTcMN && b.k >= kTcK;

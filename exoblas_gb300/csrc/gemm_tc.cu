@@ -614,6 +614,11 @@ static TcGroupState *group_create(const TcGroupOp *ops, int n) {
   // longest tiles first; ties keep product and raster order (stable)
   std::stable_sort(items.begin(), items.end(),
                    [](const std::pair<int, TcItem> &a, const std::pair<int, TcItem> &b) { return a.first > b.first; });
+  if (first > 0x7fffffffL) {
+    cudaFree(st->planes);
+    delete st;
+    fail(EXOBLAS_INVALID_VALUE, "tensor-core batch: too many split tiles for one launch");
+  }
   std::vector<TcItem> it(items.size());
   for (size_t i = 0; i < items.size(); ++i) it[i] = items[i].second;
   st->nitems = int(it.size());
